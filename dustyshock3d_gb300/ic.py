@@ -1,0 +1,202 @@
+"""Initial conditions.
+
+``init_sod_x_dust`` restates the reference's active generator
+(kernel.cu:1391-1582) so that a reference run can be replayed from identical
+FP64 inputs, including its quirks:
+
+* the ``Ind`` flag is assigned outside the accept test (kernel.cu:1441-1448,
+  1481-1488), so a rejected lattice point overwrites the flag of the last
+  accepted particle;
+* the interior test uses ``X_cube`` for y (kernel.cu:1441, 1481);
+* ``Coeff_h_dust_cell`` is forced to 0.5 (kernel.cu:1498).
+
+A rejected point before the first accepted one makes the reference write
+``Ind_gas[-1]``; that is undefined behaviour there and rejected here.
+
+``dusty_sod_tube`` builds the dusty Sod shock tube of the benchmark
+configurations (no reference counterpart): two cubic lattices with equal
+particle mass, dust on the same lattices offset by half a spacing, h = 1.3
+local spacing, periodic y/z, frozen walls at the x ends.
+"""
+from __future__ import annotations
+
+import math
+from typing import List, Tuple
+
+import numpy as np
+
+from .params import Mode, Params
+from .species import Species
+
+
+def _eq_state(rho, e, type_of_state, gam, cs):
+    """kernel.cu:92-97."""
+    if type_of_state == 1:
+        return cs * cs * rho
+    return rho * e * (gam - 1)
+
+
+def _lattice(x0, sign, dl, Im, Y_min, Jm, Z_min, Km):
+    i, j, k = np.meshgrid(np.arange(Im + 1, dtype=np.float64), np.arange(Jm + 1, dtype=np.float64),
+                          np.arange(Km + 1, dtype=np.float64), indexing="ij")
+    i = i.ravel(); j = j.ravel(); k = k.ravel()
+    if sign < 0:
+        x = 0.0 - (i * dl)
+    else:
+        x = dl + (i * dl)
+    y = Y_min + (j * dl)
+    z = Z_min + (k * dl)
+    return x, y, z
+
+
+def init_sod_x_dust(P: Params) -> Tuple[Params, List[Species]]:
+    """kernel.cu:1391-1582: gas on two lattices (e 2.5 | 2.0, rho 1 | 1) and two
+    dust species copied onto the gas positions.  Returns (params, [gas, d1, d2])."""
+    P = P.copy()
+    h = P.h
+    border_length = 2.5 * h
+    X_cube, Y_cube, Z_cube = 1.0, 0.8, 0.8
+    e_left, e_right, rho_left, rho_right = 2.5, 2.0, 1.0, 1.0
+    p_left = _eq_state(rho_left, e_left, P.Type_of_state, 1.4, 1.0)
+    p_right = _eq_state(rho_right, e_right, P.Type_of_state, 1.4, 1.0)
+    mas_particle = 1.0 / (P.Particle_on_length * P.Particle_on_length * P.Particle_on_length)
+    dlh_left = math.pow(mas_particle / rho_left, 1 / 3.0)
+    dlh_right = math.pow(mas_particle / rho_right, 1 / 3.0)
+
+    parts = []
+    Im = int((0.0 - P.X_min) / dlh_left) + 1
+    Jm = int((P.Y_max - P.Y_min) / dlh_left) + 1
+    Km = int((P.Z_max - P.Z_min) / dlh_left) + 1
+    xl, yl, zl = _lattice(0.0, -1, dlh_left, Im, P.Y_min, Jm, P.Z_min, Km)
+    parts.append((xl, yl, zl, e_left, p_left, rho_left))
+    Im = int((P.X_max - 0.0) / dlh_right) + 1
+    Jm = int((P.Y_max - P.Y_min) / dlh_right) + 1
+    Km = int((P.Z_max - P.Z_min) / dlh_right) + 1
+    xr, yr, zr = _lattice(0.0, +1, dlh_right, Im, P.Y_min, Jm, P.Z_min, Km)
+    parts.append((xr, yr, zr, e_right, p_right, rho_right))
+
+    X = np.concatenate([q[0] for q in parts])
+    Y = np.concatenate([q[1] for q in parts])
+    Z = np.concatenate([q[2] for q in parts])
+    E = np.concatenate([np.full(len(q[0]), q[3]) for q in parts])
+    PP = np.concatenate([np.full(len(q[0]), q[4]) for q in parts])
+    R = np.concatenate([np.full(len(q[0]), q[5]) for q in parts])
+    acc = (np.abs(X) <= X_cube) & (np.abs(Y) <= Y_cube) & (np.abs(Z) <= Z_cube)
+    interior = ((np.abs(X) <= X_cube - border_length) & (np.abs(Y) <= X_cube - border_length)
+                & (np.abs(Z) <= Z_cube - border_length))
+    pidx = np.cumsum(acc) - 1  # index of the last accepted particle at each lattice point
+    if len(pidx) and pidx[0] < 0:
+        raise ValueError("first lattice point rejected: the reference writes Ind_gas[-1] here "
+                         "(undefined behaviour); choose Y_min, Z_min inside the 0.8 cube")
+    N = int(acc.sum())
+    if N > P.Maximum_particle:
+        raise ValueError(f"{N} gas particles exceed Maximum_particle={P.Maximum_particle} "
+                         "(the reference would overrun its arrays, kernel.cu:1751)")
+    # Ind[p] takes the interior flag of the LAST lattice point that saw p as current
+    last = np.full(N, -1, dtype=np.int64)
+    np.maximum.at(last, pidx, np.arange(len(pidx)))
+    ind = np.where(interior[last], 0, 1).astype(np.int32)
+
+    sel = np.nonzero(acc)[0]
+    n = len(sel)
+    gas = Species(x=X[sel].copy(), y=Y[sel].copy(), z=Z[sel].copy(),
+                  vx=np.zeros(n), vy=np.zeros(n), vz=np.zeros(n),
+                  ax=np.zeros(n), ay=np.zeros(n), az=np.zeros(n),
+                  rho=R[sel].copy(), p=PP[sel].copy(), e=E[sel].copy(),
+                  m=np.full(n, mas_particle), h=np.full(n, h), ts=np.zeros(n), ind=ind)
+
+    # kernel.cu:1497-1502
+    P.Coeff_h_dust_cell = 0.5
+    P.n_dust = 2
+    P.mass_ratio = [0.75, 0.5]
+    P.R_dust = [0.01, 1.0]
+    dust = []
+    for k in range(2):
+        mr, Rd = P.mass_ratio[k], P.R_dust[k]
+        # Eq_t_stop, kernel.cu:43-46
+        ts = Rd / (np.sqrt(P.Gam_g * gas.p / gas.rho) * gas.rho)
+        dust.append(Species(x=gas.x.copy(), y=gas.y.copy(), z=gas.z.copy(),
+                            vx=np.zeros(n), vy=np.zeros(n), vz=np.zeros(n),
+                            ax=np.zeros(n), ay=np.zeros(n), az=np.zeros(n),
+                            rho=gas.rho * mr, p=np.zeros(n), e=np.zeros(n),
+                            m=gas.m * mr, h=np.full(n, h), ts=ts, ind=ind.copy()))
+    P.mode = Mode.reference()
+    return P, [gas] + dust
+
+
+def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0, t_s: float = 1e-3,
+                   rho_L: float = 1.0, p_L: float = 1.0, rho_R: float = 0.125, p_R: float = 0.1,
+                   gamma: float = 1.4, h_factor: float = 1.3, x_range=(-0.5, 0.5), wall: float = 2.5,
+                   t_end: float = 0.2, cfl: float = 0.3, alpha: float = 1.0, beta: float = 2.0,
+                   av_eps: float = 0.01, idic_cells_per_right_spacing: float = 2.0,
+                   fixed_tau: float = None) -> Tuple[Params, List[Species]]:
+    """Dusty Sod tube on [x0, x1] x [0, Ly] x [0, Lz], periodic in y and z.
+
+    The left state sits on a cubic lattice of spacing ``dx_left``; the right
+    lattice has n_R = round(L/(dx_left*(rho_L/rho_R)^(1/3))) sites across each
+    periodic side and the same particle mass per x-slab (spacing 2 dx_left for
+    the classical density ratio 8).  One dust species sits on each lattice
+    offset by half a spacing in x, y and z, with mass eps x the gas mass.
+    Particles within ``wall`` smoothing lengths of either x end are frozen
+    (Ind = 1), like the reference's border particles (kernel.cu:1396, 1441).
+    """
+    Lz = Ly if Lz is None else Lz
+    x0, x1 = x_range
+    xm = 0.5 * (x0 + x1)
+
+    def side(rho, p, xa, xb, dxy_target, left):
+        ny = max(1, int(round(Ly / dxy_target)))
+        nz = max(1, int(round(Lz / dxy_target)))
+        dy, dz = Ly / ny, Lz / nz
+        m = rho_L * dx_left ** 3
+        dx = m / (rho * dy * dz)
+        nx = max(1, int(round((xb - xa) / dx)))
+        dx = (xb - xa) / nx
+        mass = rho * dx * dy * dz
+        hloc = h_factor * (dx * dy * dz) ** (1.0 / 3.0)
+        i, j, k = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                              np.arange(nz, dtype=np.float64), indexing="ij")
+        gx = xa + (i.ravel() + 0.5) * dx
+        gy = (j.ravel() + 0.5) * dy
+        gz = (k.ravel() + 0.5) * dz
+        # dust: offset by half a spacing (y, z wrap onto the periodic lattice)
+        dxp = gx + 0.5 * dx
+        dyp = np.mod(gy + 0.5 * dy, Ly)
+        dzp = np.mod(gz + 0.5 * dz, Lz)
+        e = p / ((gamma - 1.0) * rho)
+        return dict(gx=gx, gy=gy, gz=gz, dxp=dxp, dyp=dyp, dzp=dzp, mass=mass, h=hloc, rho=rho, p=p, e=e,
+                    dx=dx)
+
+    L = side(rho_L, p_L, x0, xm, dx_left, True)
+    R = side(rho_R, p_R, xm, x1, dx_left * (rho_L / rho_R) ** (1.0 / 3.0), False)
+
+    def build(key_x, key_y, key_z, dust):
+        xs, ys, zs, ms, hs, rs, ps, es = [], [], [], [], [], [], [], []
+        for S in (L, R):
+            n = len(S[key_x])
+            xs.append(S[key_x]); ys.append(S[key_y]); zs.append(S[key_z])
+            ms.append(np.full(n, S["mass"] * (eps if dust else 1.0)))
+            hs.append(np.full(n, S["h"]))
+            rs.append(np.full(n, S["rho"] * (eps if dust else 1.0)))
+            ps.append(np.full(n, 0.0 if dust else S["p"]))
+            es.append(np.full(n, 0.0 if dust else S["e"]))
+        x = np.concatenate(xs); n = len(x)
+        h = np.concatenate(hs)
+        ind = ((x < x0 + wall * h) | (x > x1 - wall * h)).astype(np.int32)
+        return Species(x=x, y=np.concatenate(ys), z=np.concatenate(zs), vx=np.zeros(n), vy=np.zeros(n),
+                       vz=np.zeros(n), ax=np.zeros(n), ay=np.zeros(n), az=np.zeros(n),
+                       rho=np.concatenate(rs), p=np.concatenate(ps), e=np.concatenate(es),
+                       m=np.concatenate(ms), h=h, ts=np.full(n, t_s) if dust else np.zeros(n), ind=ind)
+
+    gas = build("gx", "gy", "gz", False)
+    dust = build("dxp", "dyp", "dzp", True)
+    h_max = max(L["h"], R["h"])
+    P = Params(X_min=x0, X_max=x1, Y_min=0.0, Y_max=Ly, Z_min=0.0, Z_max=Lz, Type_of_state=0,
+               Maximum_particle=gas.n, Particle_on_length=1.0 / dx_left, h=h_max, Coeff_h_dust_cell=0.5,
+               tau=fixed_tau if fixed_tau else 1e-4, T_end=t_end, T_out=t_end, alpha=alpha, beta=beta,
+               eps=av_eps, Gam_g=gamma, Speed_of_sound_gas=1.0, n_dust=1, mass_ratio=[eps], R_dust=[0.0],
+               t_stop_const=[t_s], eps_empty=[eps], t_empty=t_s, cell_w=2.0 * h_max,
+               idic_w=idic_cells_per_right_spacing * R["dx"], cfl=cfl, mode=Mode.baseline())
+    if fixed_tau:
+        P.mode.cfl = False
+    return P, [gas, dust]
