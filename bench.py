@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-steps/s of the dusty-gas SPH + IDIC step on one GB300.
+
+Workload (default): the 720k gas + 720k dust dusty Sod shock tube (left
+dx = 1/800, cross-section 0.05 x 0.05, eps = 1, t_s = 1e-3, h = 1.3 local dx,
+CFL 0.3, periodic y/z), synthetic lattice initial conditions.  A step is one
+time step of every particle.  The state (~370 MB resident) is larger than L2,
+so no flush is needed between timed steps.
+
+Reported (one JSON line from rank 0):
+  value      FP32 path (FP32 neighbour sums, Kahan; FP64 state, IDIC, sums),
+             device-resident, CUDA events around exactly --steps steps
+  fp64       the plain FP64 path (reference operation order) on the same tube
+  l1_*       L1 error of the FP32 path against the FP64 path after the run
+  e2e        the same metric through the C ABI with host buffers: every step
+             uploads the full particle state from pinned memory, steps once,
+             and downloads the full state
+  roofline   the force sweep (dominant kernel): compulsory bytes / duration
+  cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on a bounded sample
+
+--impl reference times the reference algorithm on the host cores (the oracle,
+a CPU restatement of the reference's step; the reference's own GPU program
+cannot be built on the GPU host from this repository).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (dx_left, Ly, description)
+    "dusty_sod_720k": (1 / 800, 0.05, "dusty Sod tube, 720k gas + 720k dust (left dx 1/800, 0.05^2 cross-section)"),
+    "dusty_sod_45k": (1 / 200, 0.1, "dusty Sod tube, 45k gas + 45k dust (left dx 1/200, 0.1^2 cross-section)"),
+    "dusty_sod_5760k": (1 / 1600, 0.05, "dusty Sod tube, 5.76M gas + 5.76M dust (left dx 1/1600, 0.05^2)"),
+}
+DEFAULT_WORKLOAD = "dusty_sod_720k"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def make_tube(name, ly_scale=1.0):
+    from dustyshock3d_gb300 import ic
+    dx, Ly, _ = WORKLOADS[name]
+    return ic.dusty_sod_tube(dx_left=dx, Ly=Ly * ly_scale, eps=1.0, t_s=1e-3)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        loaded = [v for v in sm if v > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (one process per GPU, replicas of the tube)
+# ---------------------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devs = vis.split(",") if vis else [str(i) for i in range(64)]
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local]
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return ws, rank, dist
+    return 1, 0, None
+
+
+def dist_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle (reference algorithm restated, FP64, OpenMP)
+# ---------------------------------------------------------------------------
+def time_cpu(name, steps, budget_s=25.0):
+    """Oracle steps on all host cores; shrinks the tube cross-section if one
+    step would not fit the budget.  Returns (particle-steps/s, sample text)."""
+    from oracle.oracle import OracleState
+    scale = 1.0
+    P, sp = make_tube(name, scale)
+    O = OracleState(P, sp)
+    t0 = time.perf_counter()
+    O.step(1)
+    t1 = time.perf_counter() - t0
+    n = sum(s.n for s in sp)
+    done, el = 1, t1
+    while done < steps and el + t1 <= budget_s:
+        t0 = time.perf_counter()
+        O.step(1)
+        el += time.perf_counter() - t0
+        done += 1
+    return n * done / el, f"{done} FP64 step(s) of the full {n}-particle tube from t=0 ({el:.1f} s)", n
+
+
+def cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    ws, rank, dist = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle.oracle import OracleState
+    name = args.workload
+    P, sp = make_tube(name)
+    O = OracleState(P, sp)
+    n = sum(s.n for s in sp)
+    t0 = time.perf_counter()
+    O.step(1)
+    t_step = time.perf_counter() - t0
+    # bounded: warmup + steps must end within ~3 minutes; otherwise time a
+    # tube of smaller cross-section (same lattice spacing)
+    scale = 1.0
+    budget = 180.0
+    if t_step * (args.warmup + args.steps) > budget:
+        scale = max(0.2, (budget / (t_step * (args.warmup + args.steps))) ** 0.5)
+        P, sp = make_tube(name, scale)
+        O = OracleState(P, sp)
+        n = sum(s.n for s in sp)
+    for _ in range(max(0, args.warmup - 1)):
+        O.step(1)
+    t0 = time.perf_counter()
+    O.step(args.steps)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    sample = (f"{args.steps} FP64 oracle steps of a {n}-particle tube"
+              + ("" if scale == 1.0 else f" (cross-section scaled by {scale:.2f}^2 to fit the time budget)"))
+    line = {"metric": "particle-steps/s", "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": name, "description": WORKLOADS[name][2], "particles": n},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(path):
+    """DRAM bytes per launch of the force sweep from a committed ncu summary."""
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_particle:"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def force_bytes_per_particle(fp32: bool, hpp: bool) -> int:
+    """Compulsory bytes of one force-sweep launch per gas particle (each input
+    array read once, each output written once)."""
+    if fp32:
+        # pos32, vm32, hyd32 float4 (48) + x, y, z (24) + m, p, rho (24) + Ind (4); out ax, ay, az, edot (32)
+        return 48 + 24 + 24 + 4 + 32
+    # x, y, z, vx, vy, vz, m, rho, p-derived c and p/rho^2 (72) + h (8) + pos32 (16) + Ind (4); out 32
+    return 72 + (8 if hpp else 0) + 16 + 4 + 32
+
+
+def e2e_run(P, sp, steps, warmup):
+    """Full-state upload (pinned) + one step + full-state download, per step."""
+    import ctypes
+
+    import numpy as np
+
+    from dustyshock3d_gb300 import _lib
+    from dustyshock3d_gb300.solver import Solver
+    L = _lib.load()
+    keep = []
+
+    def pinned(n, dtype):
+        ptr = ctypes.c_void_p()
+        nbytes = n * np.dtype(dtype).itemsize
+        _lib.check(L, None, L.ds_host_alloc(ctypes.byref(ptr), nbytes), "ds_host_alloc")
+        keep.append(ptr)
+        buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+        return np.frombuffer(buf, dtype=dtype, count=n)
+
+    S = Solver(P)
+    S.set_tube(0, sp)
+    g, d = sp[0].copy().fill_missing(), sp[1].copy().fill_missing()
+    gin = {f: pinned(g.n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p",
+                                                 "e", "m", "h")}
+    din = {f: pinned(d.n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "m", "ts", "h")}
+    gind, dind = pinned(g.n, np.int32), pinned(d.n, np.int32)
+    for f, a in gin.items():
+        a[:] = getattr(g, f)
+    for f, a in din.items():
+        a[:] = getattr(d, f)
+    gind[:] = g.ind
+    dind[:] = d.ind
+    gout = {f: gin[f] for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e")}
+    dout = {f: din[f] for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")}
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
+    h2d = sum(a.nbytes for a in gin.values()) + sum(a.nbytes for a in din.values()) + gind.nbytes + dind.nbytes
+    d2h = sum(a.nbytes for a in gout.values()) + sum(a.nbytes for a in dout.values()) + gind.nbytes + dind.nbytes
+
+    def one():
+        c = S.ctx
+        _lib.check(L, c, L.ds_upload_gas(c, g.n, *[dp(gin[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay",
+                                                                         "az", "rho", "p", "e", "m", "h")], ip(gind)),
+                   "upload gas")
+        _lib.check(L, c, L.ds_upload_dust(c, 1, d.n, *[dp(din[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "rho",
+                                                                            "m", "ts", "h")], ip(dind)),
+                   "upload dust")
+        _lib.check(L, c, L.ds_step(c, 1), "step")
+        _lib.check(L, c, L.ds_download_gas(c, *[dp(gout[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay",
+                                                                      "az", "rho", "p", "e")], ip(gind)),
+                   "download gas")
+        _lib.check(L, c, L.ds_download_dust(c, 1, *[dp(dout[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "rho",
+                                                                          "ts")], ip(dind)), "download dust")
+
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    el = time.perf_counter() - t0
+    S.close()
+    for p in keep:
+        L.ds_host_free(p)
+    return el, h2d, d2h
+
+
+def run_ours(args):
+    ws, rank, dist = dist_setup()
+    import numpy as np
+
+    from dustyshock3d_gb300.solver import Solver
+    name = args.workload
+    P, sp = make_tube(name)
+    n = sum(s.n for s in sp)
+    n_gas = sp[0].n
+    clocks = ClockSampler(0)
+    clocks.start()
+
+    # FP32 path: the headline
+    P32 = P.copy()
+    P32.precision = "fp32"
+    S = Solver(P32)
+    S.set_tube(0, sp)
+    S.step(args.warmup)
+    barrier(dist)
+    total_ms, phase = S.step_timed(args.steps)
+    total_ms = dist_max(dist, total_ms)
+    kps = S.kernels_per_step()
+    g32 = S.get_species(0, 0)
+    d32 = S.get_species(0, 1)
+    t32 = S.time(0)
+    S.close()
+
+    fp64 = None
+    if not args.no_fp64:
+        S = Solver(P)
+        S.set_tube(0, sp)
+        S.step(args.warmup)
+        barrier(dist)
+        ms64, phase64 = S.step_timed(args.steps)
+        ms64 = dist_max(dist, ms64)
+        g64 = S.get_species(0, 0)
+        d64 = S.get_species(0, 1)
+        t64 = S.time(0)
+        S.close()
+        fp64 = {"value": ws * n * args.steps / (ms64 * 1e-3), "ms_per_step": ms64 / args.steps,
+                "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
+                                                                          phase64)}}
+        rel = lambda a, b: float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))  # noqa: E731
+        fp64["l1_fp32_vs_fp64"] = {"rho_gas": rel(g32.rho, g64.rho), "v_gas": rel(g32.vx, g64.vx),
+                                   "v_dust": rel(d32.vx, d64.vx), "t_fp32": t32[0], "t_fp64": t64[0],
+                                   "steps": args.warmup + args.steps}
+
+    e2e = None
+    if not args.no_e2e:
+        barrier(dist)
+        el, h2d, d2h = e2e_run(P32, sp, args.steps, min(args.warmup, 2))
+        el = dist_max(dist, el)
+        e2e = {"value": ws * n * args.steps / el, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / args.steps,
+               "path": "ds_upload_gas/dust (pinned) + ds_step(1) + ds_download_gas/dust, fp32 path"}
+    clk = clocks.stop()
+
+    if rank != 0:
+        return 0
+    value = ws * n * args.steps / (total_ms * 1e-3)
+    peak, peak_kind = peak_hbm()
+    force_ms = phase[2] / args.steps
+    bpp = force_bytes_per_particle(True, P.mode.h_per_particle)
+    achieved = bpp * n_gas / (force_ms * 1e-3) / 1e9
+    tr = profile_traffic(os.path.join(ROOT, "profiles", "force32_dusty_sod_720k.txt"))
+    roof = {"kernel": "k_force32 (force + energy-rate sweep, FP32)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": None if tr is None else tr * n_gas,
+            "algorithmic_bytes_per_launch": bpp * n_gas, "avg_launch_ms": force_ms,
+            "note": "the sweep is FP32-issue bound, not HBM bound (candidates from 27 cells per particle)"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, sample, _ = time_cpu(name, 3)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": cores(), "kind": "port", "sample": sample}
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": name, "description": WORKLOADS[name][2], "particles": n, "gas": n_gas,
+                       "precision": "fp32 neighbour sums (Kahan), fp64 state / IDIC / sums",
+                       "l2": "inputs larger than L2 (resident state ~%d MB)" % (n * 256 // 2 ** 20),
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single tube"},
+            "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
+                                                                     phase)},
+            "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "gpu_launches": kps * args.steps, "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

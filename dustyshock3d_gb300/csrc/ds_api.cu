@@ -1,0 +1,858 @@
+// ds_api.cu -- the C ABI (include/dustyshock3d_gb300.h): contexts, resident
+// device state, the step sequence and its CUDA graphs.
+//
+// The reference runs each step as ~120 launches with a device sync after each
+// and ~35 blocking copies (kernel.cu:1929-2566), building cell lists and doing
+// the IDIC cell algebra on the host.  Here one step is ~25 launches on one
+// stream with no host work and no copies; the sequence is captured once into a
+// CUDA graph per buffer parity and replayed.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/dustyshock3d_gb300.h"
+#include "ds_common.cuh"
+#include "ds_kernels.cuh"
+#include "ds_sort.cuh"
+
+#define DS_VERSION "dustyshock3d_gb300 1.0 (sm_103a)"
+
+namespace {
+
+struct HostSpecies {
+  int n = -1;
+  std::vector<double> f[15];  // x y z vx vy vz ax ay az rho p e m h ts
+  std::vector<int> ind;
+};
+
+enum { FX, FY, FZ, FVX, FVY, FVZ, FAX, FAY, FAZ, FRHO, FP, FE, FM, FH, FTS, NF };
+
+struct Buffers {
+  double *f[NF] = {};
+  int *ind = nullptr, *pid = nullptr;
+  DevState view() const {
+    DevState s;
+    s.x = f[FX]; s.y = f[FY]; s.z = f[FZ]; s.vx = f[FVX]; s.vy = f[FVY]; s.vz = f[FVZ];
+    s.ax = f[FAX]; s.ay = f[FAY]; s.az = f[FAZ]; s.rho = f[FRHO]; s.p = f[FP]; s.e = f[FE];
+    s.m = f[FM]; s.h = f[FH]; s.ts = f[FTS]; s.ind = ind; s.pid = pid;
+    return s;
+  }
+};
+
+}  // namespace
+
+struct ds_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int ntubes = 0;
+  std::vector<ds_params> params;
+  std::vector<std::vector<HostSpecies>> host;  // [tube][species]
+  bool finalized = false;
+  std::string msg;
+  // sizes
+  int N = 0;
+  int nkeys = 0, key_bits = 0, nikeys = 0, ikey_bits = 0, ncell_total = 0, nseg = 0;
+  std::vector<TubeDesc> tdesc;
+  std::vector<Chunk> ch_all, ch_gas, ch_dust;
+  // device
+  std::vector<void *> allocs;
+  long long bytes = 0;
+  Buffers buf[2];
+  int parity = 0;
+  TubeDesc *d_tubes = nullptr;
+  TubeState *d_tstate = nullptr;
+  Chunk *d_ch_all = nullptr, *d_ch_gas = nullptr, *d_ch_dust = nullptr;
+  int *d_seg_key0 = nullptr, *d_seg_species = nullptr, *d_seg_orphan = nullptr, *d_tube_cell0 = nullptr;
+  float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
+  double *cs64 = nullptr, *pt64 = nullptr, *edot = nullptr;
+  uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
+  uint32_t *ikin = nullptr, *ivin = nullptr, *ikalt = nullptr, *ivalt = nullptr;
+  uint32_t *rs_scratch = nullptr;
+  int *slot_of_pid = nullptr, *ind_of_pid = nullptr, *idic_local = nullptr, *cell_start = nullptr;
+  int *ncand = nullptr, *nnb = nullptr, *dbg_head = nullptr, *dbg_next = nullptr, *dbg_key = nullptr;
+  double *stage = nullptr;  // N doubles, download/upload staging
+  double *d_cons = nullptr;
+  int *d_flags = nullptr;
+  CellArrays ca{};
+  bool sort_alt = false, isort_alt = false;
+  bool any_hpp = false, any_proper = false, any_dust_rho = false, any_fp32 = false;
+  // graphs
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // timing
+  cudaEvent_t ev[DS_NPHASE + 1] = {};
+  std::vector<cudaEvent_t> tev;
+};
+
+namespace {
+
+ds_status fail(ds_ctx *c, ds_status st, const std::string &m) {
+  if (c) c->msg = m;
+  return st;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(c, e_ == cudaErrorMemoryAllocation ? DS_ERR_NOMEM : DS_ERR_CUDA,            \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+template <class T> ds_status dalloc(ds_ctx *c, T **p, size_t count) {
+  size_t bytes = sizeof(T) * (count ? count : 1);
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return fail(c, DS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  c->bytes += (long long)bytes;
+  *p = (T *)q;
+  return DS_OK;
+}
+
+#define DA(ptr, count)                         \
+  do {                                         \
+    ds_status s_ = dalloc(c, &(ptr), (count)); \
+    if (s_ != DS_OK) return s_;                \
+  } while (0)
+
+int bits_for(long long n) {
+  int b = 1;
+  while ((1LL << b) < n) b++;
+  return b;
+}
+
+// Tube constants from its parameters; grid sizes follow kernel.cu:1767-1778
+// and kernel.cu:1577-1582 with the same arithmetic.
+void build_desc(const ds_params &P, TubeDesc &T) {
+  memset(&T, 0, sizeof(T));
+  T.mode = P.mode;
+  T.ox = P.X_min; T.oy = P.Y_min; T.oz = P.Z_min;
+  const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;
+  T.Cnx = (int)((P.X_max - P.X_min) / w);
+  T.Cny = (int)((P.Y_max - P.Y_min) / w);
+  T.Cnz = (int)((P.Z_max - P.Z_min) / w);
+  T.Ly = P.Y_max - P.Y_min;
+  T.Lz = P.Z_max - P.Z_min;
+  T.ymax = P.Y_max; T.zmax = P.Z_max;
+  T.wx = T.wy = T.wz = w;
+  const bool proper = (P.mode & DS_MODE_GRID_PROPER) != 0;
+  if (!proper) {
+    T.sy = T.Cnx;
+    T.sz = T.Cnx * T.Cny;
+    T.ncells = (T.Cnx + 1) * (T.Cny + 1) * (T.Cnz + 1);
+    T.nx = T.Cnx + 1; T.ny = T.Cny + 1; T.nz = T.Cnz + 1;
+  } else {
+    T.nx = T.Cnx + 1;
+    T.ny = (P.mode & DS_MODE_PERIODIC_Y) ? (int)(T.Ly / w) : T.Cny + 1;
+    T.nz = (P.mode & DS_MODE_PERIODIC_Z) ? (int)(T.Lz / w) : T.Cnz + 1;
+    if (T.ny < 1) T.ny = 1;
+    if (T.nz < 1) T.nz = 1;
+    if (P.mode & DS_MODE_PERIODIC_Y) T.wy = T.Ly / T.ny;
+    if (P.mode & DS_MODE_PERIODIC_Z) T.wz = T.Lz / T.nz;
+    T.sy = T.nx;
+    T.sz = T.nx * T.ny;
+    T.ncells = T.nx * T.ny * T.nz;
+  }
+  T.aw = P.idic_w > 0 ? P.idic_w : P.Coeff_h_dust_cell * P.h;
+  T.Nax = (int)((P.X_max - P.X_min) / T.aw);
+  T.Nay = (int)((P.Y_max - P.Y_min) / T.aw);
+  T.Naz = (int)((P.Z_max - P.Z_min) / T.aw);
+  T.n_idic = (T.Nax + 1) * (T.Nay + 1) * (T.Naz + 1);
+  T.anx = T.Nax + 1; T.any_ = T.Nay + 1; T.anz = T.Naz + 1;
+  if (P.mode & DS_MODE_IDIC_PROPER) {
+    T.asy = T.anx;
+    T.asz = T.anx * T.any_;
+  } else {
+    T.asy = T.Nax;
+    T.asz = T.Nax * T.Nay;
+  }
+  T.h = P.h; T.alpha = P.alpha; T.beta = P.beta; T.eps = P.eps; T.gam = P.Gam_g;
+  T.cs = P.Speed_of_sound_gas; T.tau = P.tau; T.cfl = P.cfl; T.t_end = P.T_end; T.t_empty = P.t_empty;
+  T.type_of_state = P.Type_of_state; T.n_dust = P.n_dust; T.precision = P.precision;
+  for (int k = 0; k < DS_MAXD; k++) {
+    T.mass_ratio[k] = P.mass_ratio[k]; T.R_dust[k] = P.R_dust[k];
+    T.t_stop_const[k] = P.t_stop_const[k]; T.eps_empty[k] = P.eps_empty[k];
+  }
+  T.fx = 0.5 * (P.X_min + P.X_max);
+  T.fy = 0.5 * (P.Y_min + P.Y_max);
+  T.fz = 0.5 * (P.Z_min + P.Z_max);
+  T.cellrel = proper ? 1 : 0;
+  double L = fmax(P.X_max - P.X_min, fmax(P.Y_max - P.Y_min, P.Z_max - P.Z_min));
+  double wmax = fmax(T.wx, fmax(T.wy, T.wz));
+  // FP32 screen slack: rounding of |coordinate| <= L (or <= 2 cell widths when
+  // cell-relative) in each of the two operands, with a 5x margin
+  T.pre_abs = (float)(1e-6 * (proper ? 4.0 * wmax : L));
+}
+
+ds_status check_params(ds_ctx *c, const ds_params &P) {
+  if (P.n_dust < 1 || P.n_dust > DS_MAX_DUST) return fail(c, DS_ERR_ARG, "n_dust must be 1..4");
+  if (!(P.h > 0)) return fail(c, DS_ERR_ARG, "h must be positive");
+  if (P.Type_of_state != 0 && P.Type_of_state != 1) return fail(c, DS_ERR_ARG, "Type_of_state must be 0 or 1");
+  if (P.precision != DS_PRECISION_FP64 && P.precision != DS_PRECISION_FP32)
+    return fail(c, DS_ERR_ARG, "precision must be 0 (fp64) or 1 (fp32)");
+  if ((P.precision == DS_PRECISION_FP32) && !(P.mode & DS_MODE_GRID_PROPER))
+    return fail(c, DS_ERR_UNSUPPORTED, "the fp32 path needs the proper cell grid (DS_MODE_GRID_PROPER)");
+  if (((P.mode & (DS_MODE_PERIODIC_Y | DS_MODE_PERIODIC_Z)) != 0) && !(P.mode & DS_MODE_GRID_PROPER))
+    return fail(c, DS_ERR_UNSUPPORTED, "periodic axes need the proper cell grid (DS_MODE_GRID_PROPER)");
+  TubeDesc T;
+  build_desc(P, T);
+  if (T.Cnx < 0 || T.Cny < 0 || T.Cnz < 0) return fail(c, DS_ERR_ARG, "box extent must be positive");
+  if (T.ncells <= 0 || T.ncells > (1 << 28)) return fail(c, DS_ERR_ARG, "neighbour grid too large");
+  if (T.n_idic <= 0 || T.n_idic > (1 << 28)) return fail(c, DS_ERR_ARG, "IDIC grid too large");
+  if ((P.mode & DS_MODE_PERIODIC_Y) && T.ny < 3) return fail(c, DS_ERR_ARG, "periodic y needs >= 3 cells");
+  if ((P.mode & DS_MODE_PERIODIC_Z) && T.nz < 3) return fail(c, DS_ERR_ARG, "periodic z needs >= 3 cells");
+  return DS_OK;
+}
+
+void add_chunks(std::vector<Chunk> &v, int tube, int s, int b, int e) {
+  for (int q = b; q < e; q += DS_CHUNK) v.push_back(Chunk{tube, s, q, q + DS_CHUNK < e ? q + DS_CHUNK : e});
+}
+
+template <class T> ds_status upload_vec(ds_ctx *c, T **dptr, const std::vector<T> &v) {
+  DA(*dptr, v.size());
+  if (!v.empty()) CK(cudaMemcpy(*dptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return DS_OK;
+}
+
+SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
+  SweepArgs a;
+  a.tubes = c->d_tubes;
+  a.tstate = c->d_tstate;
+  a.chunks = chunks;
+  a.nchunks = nchunks;
+  a.st = c->buf[c->parity].view();
+  a.cell_start = c->cell_start;
+  a.pos32 = c->pos32;
+  a.vm32 = c->vm32;
+  a.hyd32 = c->hyd32;
+  a.cs64 = c->cs64;
+  a.pt64 = c->pt64;
+  a.edot = c->edot;
+  a.ncand = c->ncand;
+  a.nnb = c->nnb;
+  a.gas_slot_of_pid = c->slot_of_pid;
+  a.gas_ind_pid = c->ind_of_pid;
+  a.tstate_rw = c->d_tstate;
+  a.flags = c->d_flags;
+  return a;
+}
+
+// Sort + reorder + cell ranges for the particles' current positions; flips parity.
+void enqueue_sort(ds_ctx *c) {
+  cudaStream_t s = c->stream;
+  DevState src = c->buf[c->parity].view();
+  DevState dst = c->buf[c->parity ^ 1].view();
+  ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, s);
+  bool alt = false;
+  ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits, c->rs_scratch, s, &alt);
+  const uint32_t *skey = alt ? c->kalt : c->kin;
+  const uint32_t *sval = alt ? c->valt : c->vin;
+  ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, src, dst, c->pos32, c->vm32,
+                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, s);
+  ds_launch_cell_start(skey, c->N, c->nkeys, c->cell_start, s);
+  c->parity ^= 1;
+}
+
+// The step after the sort: sweeps, IDIC, update.  ev: optional phase events.
+void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
+  cudaStream_t s = c->stream;
+  bool alt = false;
+  ds_radix_sort(c->ikin, c->ivin, c->ikalt, c->ivalt, c->N, c->ikey_bits, c->rs_scratch, s, &alt);
+  c->isort_alt = alt;
+  cudaMemsetAsync(c->ca.cnt, 0, sizeof(int) * (size_t)c->nikeys, s);
+  if (ev) cudaEventRecord(ev[1], s);
+  const bool fp32 = c->any_fp32;
+  SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
+  SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
+  if (fp32) ds_launch_density32(ag, c->any_hpp, 0, s);
+  else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
+  if (c->any_dust_rho) {
+    if (fp32) ds_launch_density32(ad, c->any_hpp, 1, s);
+    else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
+  }
+  DevState st = c->buf[c->parity].view();
+  ds_launch_tstop(c->d_tubes, c->d_tstate, c->d_ch_dust, (int)c->ch_dust.size(), st, c->slot_of_pid, c->d_flags, s);
+  ds_launch_dt(c->d_tubes, c->d_tstate, c->ntubes, s);
+  if (ev) cudaEventRecord(ev[2], s);
+  if (fp32) ds_launch_force32(ag, c->any_hpp, s);
+  else ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
+  if (ev) cudaEventRecord(ev[3], s);
+  const uint32_t *ik = alt ? c->ikalt : c->ikin;
+  const uint32_t *iv = alt ? c->ivalt : c->ivin;
+  ds_launch_idic_reduce(ik, iv, c->N, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st, c->ca, s);
+  ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, s);
+  ds_launch_relax_move(c->d_tubes, c->d_tstate, c->d_ch_all, (int)c->ch_all.size(), st, c->idic_local, c->edot,
+                       c->ca, c->d_flags, s);
+  ds_launch_step_end(c->d_tstate, c->ntubes, s);
+}
+
+void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
+  if (ev) cudaEventRecord(ev[0], c->stream);
+  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->stream);
+  enqueue_sort(c);
+  enqueue_physics(c, ev);
+  if (ev) cudaEventRecord(ev[4], c->stream);
+}
+
+ds_status finalize(ds_ctx *c) {
+  if (c->finalized) return DS_OK;
+  CK(cudaSetDevice(c->device));
+  // segments, keys
+  c->tdesc.assign(c->ntubes, TubeDesc{});
+  std::vector<int> seg_key0, seg_species, seg_orphan, tube_cell0;
+  int N = 0;
+  long long nkeys = 0, nikeys = 0, ncell = 0;
+  for (int t = 0; t < c->ntubes; t++) {
+    const ds_params &P = c->params[t];
+    TubeDesc &T = c->tdesc[t];
+    build_desc(P, T);
+    const int ns = 1 + P.n_dust;
+    for (int s = 0; s < ns; s++) {
+      const HostSpecies &H = c->host[t][s];
+      if (H.n < 0)
+        return fail(c, DS_ERR_STATE, "tube " + std::to_string(t) + " species " + std::to_string(s) + " not set");
+      T.seg_begin[s] = N;
+      N += H.n;
+      T.seg_end[s] = N;
+      T.key_base[s] = (int)nkeys;
+      nkeys += T.ncells + 2;
+      T.idic_base[s] = (int)nikeys;
+      seg_key0.push_back((int)nikeys);
+      seg_species.push_back(s);
+      seg_orphan.push_back((int)nikeys + T.n_idic + 1);
+      nikeys += T.n_idic + 2;
+      add_chunks(c->ch_all, t, s, T.seg_begin[s], T.seg_end[s]);
+      add_chunks(s == 0 ? c->ch_gas : c->ch_dust, t, s, T.seg_begin[s], T.seg_end[s]);
+    }
+    tube_cell0.push_back((int)ncell);
+    ncell += T.n_idic + 1;
+    if (P.mode & DS_MODE_H_PER_PARTICLE) c->any_hpp = true;
+    if (P.mode & DS_MODE_GRID_PROPER) c->any_proper = true;
+    if (P.mode & DS_MODE_DUST_RHO) c->any_dust_rho = true;
+    if (P.precision == DS_PRECISION_FP32) c->any_fp32 = true;
+  }
+  if (nkeys >= (1LL << 31) || nikeys >= (1LL << 31)) return fail(c, DS_ERR_ARG, "key space too large");
+  // one kernel variant per batch: the mode bits that select templates must agree
+  for (int t = 1; t < c->ntubes; t++) {
+    const ds_params &P = c->params[t];
+    if (((P.mode & DS_MODE_H_PER_PARTICLE) != 0) != c->any_hpp || ((P.mode & DS_MODE_GRID_PROPER) != 0) != c->any_proper ||
+        (P.precision == DS_PRECISION_FP32) != c->any_fp32 || ((P.mode & DS_MODE_DUST_RHO) != 0) != c->any_dust_rho)
+      return fail(c, DS_ERR_UNSUPPORTED, "tubes of one batch must share h mode, grid kind, dust-rho mode and precision");
+  }
+  c->N = N;
+  c->nkeys = (int)nkeys;
+  c->key_bits = bits_for(nkeys);
+  c->nikeys = (int)nikeys;
+  c->ikey_bits = bits_for(nikeys);
+  c->ncell_total = (int)ncell;
+  c->nseg = (int)seg_key0.size();
+  // device memory
+  for (int b = 0; b < 2; b++) {
+    for (int f = 0; f < NF; f++) DA(c->buf[b].f[f], N);
+    DA(c->buf[b].ind, N);
+    DA(c->buf[b].pid, N);
+  }
+  DA(c->pos32, N); DA(c->vm32, N); DA(c->hyd32, N);
+  DA(c->cs64, N); DA(c->pt64, N); DA(c->edot, N);
+  DA(c->kin, N); DA(c->vin, N); DA(c->kalt, N); DA(c->valt, N);
+  DA(c->ikin, N); DA(c->ivin, N); DA(c->ikalt, N); DA(c->ivalt, N);
+  DA(c->rs_scratch, ds_radix_scratch_words(N));
+  DA(c->slot_of_pid, N); DA(c->ind_of_pid, N); DA(c->idic_local, N);
+  DA(c->cell_start, (size_t)nkeys + 1);
+  DA(c->ncand, N); DA(c->nnb, N);
+  DA(c->stage, N);
+  DA(c->d_cons, 8);
+  DA(c->d_flags, 1);
+  DA(c->ca.cnt, nikeys);
+  double **cd[] = {&c->ca.vx, &c->ca.vy, &c->ca.vz, &c->ca.a0, &c->ca.a1, &c->ca.a2,
+                   &c->ca.nvx, &c->ca.nvy, &c->ca.nvz, &c->ca.px, &c->ca.py, &c->ca.pz};
+  for (double **p : cd) DA(*p, nikeys);
+  CK(cudaMemsetAsync(c->ca.cnt, 0, sizeof(int) * (size_t)nikeys, c->stream));
+  for (double **p : cd) CK(cudaMemsetAsync(*p, 0, sizeof(double) * (size_t)nikeys, c->stream));
+  CK(cudaMemsetAsync(c->edot, 0, sizeof(double) * (size_t)(N ? N : 1), c->stream));
+  CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+  // tables
+  ds_status st;
+  if ((st = upload_vec(c, &c->d_tubes, c->tdesc)) != DS_OK) return st;
+  std::vector<TubeState> ts(c->ntubes);
+  for (auto &x : ts) memset(&x, 0, sizeof(x));
+  if ((st = upload_vec(c, &c->d_tstate, ts)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_ch_all, c->ch_all)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_ch_gas, c->ch_gas)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_ch_dust, c->ch_dust)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_seg_key0, seg_key0)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_seg_species, seg_species)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_seg_orphan, seg_orphan)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_tube_cell0, tube_cell0)) != DS_OK) return st;
+  // particles: slot = segment begin + caller index
+  c->parity = 0;
+  for (int t = 0; t < c->ntubes; t++)
+    for (int s = 0; s <= c->params[t].n_dust; s++) {
+      HostSpecies &H = c->host[t][s];
+      const int b = c->tdesc[t].seg_begin[s];
+      for (int f = 0; f < NF; f++)
+        if (H.n) CK(cudaMemcpy(c->buf[0].f[f] + b, H.f[f].data(), sizeof(double) * H.n, cudaMemcpyHostToDevice));
+      std::vector<int> pid(H.n);
+      for (int i = 0; i < H.n; i++) pid[i] = i;
+      if (H.n) {
+        CK(cudaMemcpy(c->buf[0].ind + b, H.ind.data(), sizeof(int) * H.n, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->buf[0].pid + b, pid.data(), sizeof(int) * H.n, cudaMemcpyHostToDevice));
+      }
+      for (int f = 0; f < NF; f++) { std::vector<double>().swap(H.f[f]); }
+      std::vector<int>().swap(H.ind);
+    }
+  for (int k = 0; k <= DS_NPHASE; k++) CK(cudaEventCreate(&c->ev[k]));
+  CK(cudaStreamSynchronize(c->stream));
+  c->finalized = true;
+  return DS_OK;
+}
+
+ds_status capture_graph(ds_ctx *c, int parity) {
+  if (c->graph[parity]) return DS_OK;
+  const int saved = c->parity;
+  c->parity = parity;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(c, nullptr);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->parity = saved;
+  if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&c->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return DS_OK;
+}
+
+ds_status check_flags(ds_ctx *c) {
+  int f = 0;
+  CK(cudaMemcpy(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (f) return fail(c, DS_ERR_DEVICE, "device flags set: " + std::to_string(f));
+  return DS_OK;
+}
+
+ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fields, const int *ind) {
+  if (!c) return DS_ERR_ARG;
+  if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
+  if (s < 0 || s > c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "bad species index");
+  if (n < 0) return fail(c, DS_ERR_ARG, "negative particle count");
+  if (s == 0 && n > c->params[tube].Maximum_particle && c->params[tube].Maximum_particle > 0)
+    return fail(c, DS_ERR_ARG, "gas count exceeds Maximum_particle (kernel.cu:1751)");
+  const int req[] = {FX, FY, FZ, FVX, FVY, FVZ, FRHO, FM};
+  for (int f : req)
+    if (n > 0 && !fields[f]) return fail(c, DS_ERR_ARG, "required array is NULL");
+  if (n > 0 && !ind) return fail(c, DS_ERR_ARG, "ind is NULL");
+  if (!c->finalized) {
+    HostSpecies &H = c->host[tube][s];
+    H.n = n;
+    for (int f = 0; f < NF; f++) {
+      if (fields[f]) H.f[f].assign(fields[f], fields[f] + n);
+      else if (f == FH) H.f[f].assign(n, c->params[tube].h);
+      else H.f[f].assign(n, 0.0);
+    }
+    H.ind.assign(ind, ind + n);
+    return DS_OK;
+  }
+  // resident state: overwrite this segment in caller order (the next step sorts)
+  const TubeDesc &T = c->tdesc[tube];
+  if (n != T.seg_end[s] - T.seg_begin[s]) return fail(c, DS_ERR_STATE, "particle count differs from the resident state");
+  CK(cudaSetDevice(c->device));
+  Buffers &B = c->buf[c->parity];
+  const int b = T.seg_begin[s];
+  for (int f = 0; f < NF; f++) {
+    if (fields[f]) {
+      CK(cudaMemcpyAsync(B.f[f] + b, fields[f], sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    } else if (f == FH) {
+      ds_launch_fill(B.f[f] + b, n, c->params[tube].h, c->stream);
+      CK(cudaGetLastError());
+    } else {
+      CK(cudaMemsetAsync(B.f[f] + b, 0, sizeof(double) * n, c->stream));  // absent field: zero
+    }
+  }
+  CK(cudaMemcpyAsync(B.ind + b, ind, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  ds_launch_iota(B.pid + b, n, c->stream);  // caller order: slot b + p holds particle p
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
+}
+
+__global__ void k_to_caller_order(const double *src, const int *pid, int b, int n, double *dst) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) dst[pid[b + q]] = src[b + q];
+}
+__global__ void k_to_caller_order_i(const int *src, const int *pid, int b, int n, int *dst) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) dst[pid[b + q]] = src[b + q];
+}
+
+ds_status get_species(ds_ctx *c, int tube, int s, double *const *out, int *ind_out) {
+  if (!c) return DS_ERR_ARG;
+  if (!c->finalized) return fail(c, DS_ERR_STATE, "no resident state yet (call ds_step first)");
+  if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
+  if (s < 0 || s > c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "bad species index");
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  const int b = T.seg_begin[s], n = T.seg_end[s] - b;
+  if (n == 0) return DS_OK;
+  Buffers &B = c->buf[c->parity];
+  const int nb = (n + 255) / 256;
+  for (int f = 0; f < NF; f++) {
+    if (!out[f]) continue;
+    k_to_caller_order<<<nb, 256, 0, c->stream>>>(B.f[f], B.pid, b, n, c->stage);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out[f], c->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (ind_out) {
+    k_to_caller_order_i<<<nb, 256, 0, c->stream>>>(B.ind, B.pid, b, n, (int *)c->stage);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ind_out, c->stage, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
+}
+
+// Init.txt reader (kernel.cu:1705-1723): title line, 17 leading numbers.
+ds_status read_init(const char *path, ds_params *p) {
+  FILE *f = fopen(path, "r");
+  if (!f) return DS_ERR_ARG;
+  char s[256];
+  if (!fgets(s, sizeof s, f)) { fclose(f); return DS_ERR_ARG; }
+  double *dv[] = {&p->X_min, &p->X_max, &p->Y_min, &p->Y_max, &p->Z_min, &p->Z_max};
+  int ok = 1;
+  for (double *d : dv) ok &= fgets(s, sizeof s, f) && sscanf(s, "%lf", d) == 1;
+  ok &= fgets(s, sizeof s, f) && sscanf(s, "%d", &p->Type_of_state) == 1;
+  ok &= fgets(s, sizeof s, f) && sscanf(s, "%d", &p->Maximum_particle) == 1;
+  double *dv2[] = {&p->Particle_on_length, &p->h, &p->Coeff_h_dust_cell, &p->tau, &p->T_end,
+                   &p->T_out, &p->alpha, &p->beta, &p->eps};
+  for (double *d : dv2) ok &= fgets(s, sizeof s, f) && sscanf(s, "%lf", d) == 1;
+  fclose(f);
+  return ok ? DS_OK : DS_ERR_ARG;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *ds_version(void) { return DS_VERSION; }
+
+ds_status ds_params_init(ds_params *p) {
+  if (!p) return DS_ERR_ARG;
+  memset(p, 0, sizeof(*p));
+  // Init.txt as shipped (Init.txt:2-18)
+  p->X_min = -2.0; p->X_max = 2.0; p->Y_min = -2.0; p->Y_max = 2.0; p->Z_min = -2.0; p->Z_max = 2.0;
+  p->Type_of_state = 0; p->Maximum_particle = 1000000; p->Particle_on_length = 40; p->h = 0.1;
+  p->Coeff_h_dust_cell = 0.5; p->tau = 5.0e-3; p->T_end = 0.2; p->T_out = 0.1;
+  p->alpha = 1.0; p->beta = 2.0; p->eps = 0.01;
+  p->Gam_g = 1.4;               // data.h:7
+  p->Speed_of_sound_gas = 1.0;  // kernel.cu:1744
+  p->n_dust = 2;
+  p->mode = DS_MODE_REFERENCE;
+  p->precision = DS_PRECISION_FP64;
+  p->cfl = 0.3;
+  p->t_empty = 1.0;  // kernel.cu:2160
+  p->mass_ratio[0] = 0.75; p->mass_ratio[1] = 0.5;   // kernel.cu:1499-1502
+  p->R_dust[0] = 0.01; p->R_dust[1] = 1.0;
+  p->t_stop_const[0] = p->t_stop_const[1] = 1e-3;
+  p->eps_empty[0] = 0.5; p->eps_empty[1] = 0.33;     // kernel.cu:2200, 2209
+  return DS_OK;
+}
+
+ds_status ds_params_read_init_txt(const char *path, ds_params *p) {
+  if (!path || !p) return DS_ERR_ARG;
+  return read_init(path, p);
+}
+
+ds_status ds_create_batch(int ntubes, const ds_params *p, ds_ctx **out) {
+  if (!out || !p || ntubes <= 0) return DS_ERR_ARG;
+  *out = nullptr;
+  ds_ctx *c = new ds_ctx();
+  for (int t = 0; t < ntubes; t++) {
+    ds_status st = check_params(c, p[t]);
+    if (st != DS_OK) { delete c; return st; }
+  }
+  c->ntubes = ntubes;
+  c->params.assign(p, p + ntubes);
+  c->host.resize(ntubes);
+  for (int t = 0; t < ntubes; t++) c->host[t].resize(1 + p[t].n_dust);
+  if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return DS_ERR_CUDA;
+  }
+  *out = c;
+  return DS_OK;
+}
+
+ds_status ds_create(const ds_params *p, ds_ctx **out) { return ds_create_batch(1, p, out); }
+
+ds_status ds_set_gas(ds_ctx *c, int tube, int n, const double *x, const double *y, const double *z,
+                     const double *vx, const double *vy, const double *vz, const double *ax, const double *ay,
+                     const double *az, const double *rho, const double *p, const double *e, const double *mas,
+                     const double *h, const int *ind) {
+  const double *f[NF] = {x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, mas, h, nullptr};
+  if (!c) return DS_ERR_ARG;
+  if (n > 0 && (!p || !e)) return fail(c, DS_ERR_ARG, "gas p and e are required");
+  return set_species(c, tube, 0, n, f, ind);
+}
+
+ds_status ds_set_dust(ds_ctx *c, int tube, int species, int n, const double *x, const double *y, const double *z,
+                      const double *vx, const double *vy, const double *vz, const double *rho, const double *mas,
+                      const double *t_stop, const double *h, const int *ind) {
+  if (!c) return DS_ERR_ARG;
+  if (species < 1) return fail(c, DS_ERR_ARG, "dust species are numbered from 1");
+  if (n > 0 && !t_stop) return fail(c, DS_ERR_ARG, "dust t_stop is required");
+  const double *f[NF] = {x, y, z, vx, vy, vz, nullptr, nullptr, nullptr, rho, nullptr, nullptr, mas, h, t_stop};
+  return set_species(c, tube, species, n, f, ind);
+}
+
+ds_status ds_upload_gas(ds_ctx *c, int n, const double *x, const double *y, const double *z, const double *vx,
+                        const double *vy, const double *vz, const double *ax, const double *ay, const double *az,
+                        const double *rho, const double *p, const double *e, const double *mas, const double *h,
+                        const int *ind) {
+  return ds_set_gas(c, 0, n, x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, mas, h, ind);
+}
+
+ds_status ds_upload_dust(ds_ctx *c, int species, int n, const double *x, const double *y, const double *z,
+                         const double *vx, const double *vy, const double *vz, const double *rho, const double *mas,
+                         const double *t_stop, const double *h, const int *ind) {
+  return ds_set_dust(c, 0, species, n, x, y, z, vx, vy, vz, rho, mas, t_stop, h, ind);
+}
+
+ds_status ds_step_async(ds_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  CK(cudaSetDevice(c->device));
+  for (int k = 0; k < nsteps; k++) {
+    st = capture_graph(c, c->parity);
+    if (st != DS_OK) return st;
+    CK(cudaGraphLaunch(c->graph[c->parity], c->stream));
+    c->parity ^= 1;  // the step's reorder swapped the buffers
+  }
+  return DS_OK;
+}
+
+ds_status ds_synchronize(ds_ctx *c) {
+  if (!c) return DS_ERR_ARG;
+  if (!c->finalized) return DS_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  return check_flags(c);
+}
+
+ds_status ds_step(ds_ctx *c, int nsteps) {
+  ds_status st = ds_step_async(c, nsteps);
+  if (st != DS_OK) return st;
+  return ds_synchronize(c);
+}
+
+ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms) {
+  if (!c || nsteps < 0) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  CK(cudaSetDevice(c->device));
+  // one event set per step so that the steps run back to back with a single
+  // synchronisation at the end
+  const size_t need = (size_t)nsteps * (DS_NPHASE + 1);
+  while (c->tev.size() < need) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->tev.push_back(e);
+  }
+  for (int k = 0; k < nsteps; k++) enqueue_step(c, &c->tev[(size_t)k * (DS_NPHASE + 1)]);
+  CK(cudaGetLastError());
+  float acc[DS_NPHASE] = {0, 0, 0, 0}, tot = 0;
+  if (nsteps > 0) {
+    CK(cudaEventSynchronize(c->tev[need - 1]));
+    for (int k = 0; k < nsteps; k++) {
+      cudaEvent_t *ev = &c->tev[(size_t)k * (DS_NPHASE + 1)];
+      for (int p = 0; p < DS_NPHASE; p++) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev[p], ev[p + 1]));
+        acc[p] += ms;
+      }
+    }
+    CK(cudaEventElapsedTime(&tot, c->tev[0], c->tev[need - 1]));
+  }
+  if (total_ms) *total_ms = tot;
+  if (phase_ms)
+    for (int p = 0; p < DS_NPHASE; p++) phase_ms[p] = acc[p];
+  return check_flags(c);
+}
+
+ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
+  if (!c || !count) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
+  // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
+  *count = 12 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0);
+  return DS_OK;
+}
+
+ds_status ds_get_gas(ds_ctx *c, int tube, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                     double *ax, double *ay, double *az, double *rho, double *p, double *e, int *ind) {
+  double *f[NF] = {x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, nullptr, nullptr, nullptr};
+  return get_species(c, tube, 0, f, ind);
+}
+
+ds_status ds_get_dust(ds_ctx *c, int tube, int species, double *x, double *y, double *z, double *vx, double *vy,
+                      double *vz, double *rho, double *t_stop, int *ind) {
+  if (species < 1) return fail(c, DS_ERR_ARG, "dust species are numbered from 1");
+  double *f[NF] = {x, y, z, vx, vy, vz, nullptr, nullptr, nullptr, rho, nullptr, nullptr, nullptr, nullptr, t_stop};
+  return get_species(c, tube, species, f, ind);
+}
+
+ds_status ds_download_gas(ds_ctx *c, double *x, double *y, double *z, double *vx, double *vy, double *vz, double *ax,
+                          double *ay, double *az, double *rho, double *p, double *e, int *ind) {
+  return ds_get_gas(c, 0, x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, ind);
+}
+
+ds_status ds_download_dust(ds_ctx *c, int species, double *x, double *y, double *z, double *vx, double *vy,
+                           double *vz, double *rho, double *t_stop, int *ind) {
+  return ds_get_dust(c, 0, species, x, y, z, vx, vy, vz, rho, t_stop, ind);
+}
+
+ds_status ds_get_time(ds_ctx *c, int tube, double *Tm, double *dt_last, long long *nsteps) {
+  if (!c || tube < 0 || tube >= c->ntubes) return DS_ERR_ARG;
+  if (!c->finalized) {
+    if (Tm) *Tm = 0; if (dt_last) *dt_last = 0; if (nsteps) *nsteps = 0;
+    return DS_OK;
+  }
+  TubeState ts;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(&ts, c->d_tstate + tube, sizeof(ts), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (Tm) *Tm = ts.Tm;
+  if (dt_last) *dt_last = ts.dt;
+  if (nsteps) *nsteps = ts.nstep;
+  return DS_OK;
+}
+
+ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *head, int *next, int *ncand,
+                         int *nnb, int *ncells) {
+  if (!c) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  if (tube < 0 || tube >= c->ntubes || species < 0 || species > c->params[tube].n_dust)
+    return fail(c, DS_ERR_ARG, "bad tube or species");
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  const int b = T.seg_begin[species], n = T.seg_end[species] - b;
+  if (ncells) *ncells = T.ncells;
+  enqueue_sort(c);  // lists for the current positions
+  if (ncand || nnb) {
+    std::vector<Chunk> ch;
+    add_chunks(ch, tube, species, b, b + n);
+    Chunk *d_ch = nullptr;
+    if (!ch.empty()) {
+      CK(cudaMalloc(&d_ch, sizeof(Chunk) * ch.size()));
+      CK(cudaMemcpyAsync(d_ch, ch.data(), sizeof(Chunk) * ch.size(), cudaMemcpyHostToDevice, c->stream));
+      SweepArgs a = sweep_args(c, d_ch, (int)ch.size());
+      ds_launch_counts64(a, (c->params[tube].mode & DS_MODE_H_PER_PARTICLE) != 0, c->any_proper, c->stream);
+      CK(cudaGetLastError());
+    }
+    if (ncand && n) CK(cudaMemcpyAsync(ncand, c->ncand + b, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (nnb && n) CK(cudaMemcpyAsync(nnb, c->nnb + b, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (d_ch) CK(cudaFree(d_ch));
+  }
+  if (cell_key || head || next) {
+    int *dh = nullptr, *dn = nullptr, *dk = nullptr;
+    CK(cudaMalloc(&dh, sizeof(int) * (T.ncells + 1)));
+    CK(cudaMalloc(&dn, sizeof(int) * (n > 0 ? n : 1)));
+    CK(cudaMalloc(&dk, sizeof(int) * (n > 0 ? n : 1)));
+    ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, dh, dn,
+                          dk, c->stream);
+    CK(cudaGetLastError());
+    if (head) CK(cudaMemcpyAsync(head, dh, sizeof(int) * (T.ncells + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (next && n) CK(cudaMemcpyAsync(next, dn, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (cell_key && n) CK(cudaMemcpyAsync(cell_key, dk, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(dh); cudaFree(dn); cudaFree(dk);
+  }
+  return DS_OK;
+}
+
+ds_status ds_debug_idic(ds_ctx *c, int tube, int species, int *count, double *cells, int *ncells) {
+  if (!c) return DS_ERR_ARG;
+  if (!c->finalized) return fail(c, DS_ERR_STATE, "no resident state yet (call ds_step first)");
+  if (tube < 0 || tube >= c->ntubes || species < 0 || species > c->params[tube].n_dust)
+    return fail(c, DS_ERR_ARG, "bad tube or species");
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  const int n = T.n_idic + 1, k0 = T.idic_base[species];
+  if (ncells) *ncells = n;
+  CK(cudaStreamSynchronize(c->stream));
+  if (count) CK(cudaMemcpy(count, c->ca.cnt + k0, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (cells) {
+    const double *arr[12] = {c->ca.vx, c->ca.vy, c->ca.vz, c->ca.a0, c->ca.a1, c->ca.a2,
+                             c->ca.nvx, c->ca.nvy, c->ca.nvz, c->ca.px, c->ca.py, c->ca.pz};
+    for (int k = 0; k < 12; k++)
+      CK(cudaMemcpy(cells + (size_t)k * n, arr[k] + k0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  }
+  return DS_OK;
+}
+
+ds_status ds_conservation(ds_ctx *c, int tube, double *out6) {
+  if (!c || !out6 || tube < 0 || tube >= c->ntubes) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  CK(cudaSetDevice(c->device));
+  ds_launch_conservation(c->d_tubes, tube, c->buf[c->parity].view(), c->d_cons, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out6, c->d_cons, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
+}
+
+ds_status ds_memory_bytes(ds_ctx *c, long long *bytes) {
+  if (!c || !bytes) return DS_ERR_ARG;
+  *bytes = c->bytes;
+  return DS_OK;
+}
+
+ds_status ds_last_error(ds_ctx *c, int *device_flags, char *msg, int msglen) {
+  if (!c) return DS_ERR_ARG;
+  if (device_flags) {
+    *device_flags = 0;
+    if (c->finalized) {
+      CK(cudaSetDevice(c->device));
+      CK(cudaMemcpy(device_flags, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+  }
+  if (msg && msglen > 0) {
+    strncpy(msg, c->msg.c_str(), (size_t)msglen - 1);
+    msg[msglen - 1] = 0;
+  }
+  return DS_OK;
+}
+
+ds_status ds_host_alloc(void **ptr, long long bytes) {
+  if (!ptr || bytes < 0) return DS_ERR_ARG;
+  return cudaMallocHost(ptr, (size_t)(bytes ? bytes : 1)) == cudaSuccess ? DS_OK : DS_ERR_NOMEM;
+}
+
+ds_status ds_host_free(void *ptr) { return cudaFreeHost(ptr) == cudaSuccess ? DS_OK : DS_ERR_CUDA; }
+
+void ds_destroy(ds_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int p = 0; p < 2; p++)
+    if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
+  for (int k = 0; k <= DS_NPHASE; k++)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (cudaEvent_t e : c->tev) cudaEventDestroy(e);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+}  // extern "C"

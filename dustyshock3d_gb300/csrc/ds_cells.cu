@@ -1,0 +1,537 @@
+// ds_cells.cu -- per-particle and per-cell kernels of one step (everything but
+// the neighbour sweeps and the radix sort).
+//
+// Compiled with -fmad=false: the FP64 arithmetic follows the reference's
+// operation order (IDIC.h, kernel.cu:2060-2523) without FMA contraction, so
+// the results equal the oracle's (and the reference's CPU build) bit for bit.
+//
+// Order of one step (ds_api.cu enqueues it, graph-captured):
+//   k_step_begin   per tube: active = Tm < T_end, reset the CFL minimum
+//   k_keys         neighbour key per slot, scattered to caller-index order
+//   (radix sort)   stable by key
+//   k_reorder      gather every persistent field into the sorted order; FP32
+//                  copies; IDIC key per slot, scattered to caller-index order
+//   k_cell_start   first sorted slot of every key
+//   (radix sort)   IDIC keys, stable
+//   (sweeps)       density + EOS (+ dust density), t_stop, dt, force
+//   k_idic_reduce  per IDIC cell and species: count, sum v, sum t_stop / sum A
+//   k_idic_solve   per IDIC cell: means, eps, the implicit drag solve
+//   k_relax_move   per particle: relax to the cell solution, move, energy
+//   k_step_end     per tube: Tm += dt
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ds_common.cuh"
+#include "ds_kernels.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long dbl_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+
+__global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntubes) return;
+  ts[t].active = ts[t].Tm < tubes[t].t_end ? 1 : 0;
+  ts[t].dtmin_bits = dbl_bits(__longlong_as_double(0x7ff0000000000000LL));  // +inf
+  ts[t].dt = 0.0;
+}
+
+// Neighbour key of each slot (kernel.cu:1949; out-of-range keys are not
+// listed, kernel.cu:1950, and go to the orphan bucket ncells+1), written at
+// the particle's caller index so the stable sort keeps ascending index.
+__global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
+                       uint32_t *vin) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    if (i >= ch.end) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
+    int local;
+    if (!(T.mode & M_GRID_PROPER))
+      local = (key >= 0 && key <= T.ncells) ? key : T.ncells + 1;
+    else
+      local = key >= 0 ? key : T.ncells + 1;
+    const int dst = T.seg_begin[ch.species] + st.pid[i];
+    kin[dst] = (uint32_t)(T.key_base[ch.species] + local);
+    vin[dst] = (uint32_t)i;
+  }
+}
+
+// Gather every persistent field from the previous order (src) into the new
+// sorted order (dst); build the FP32 copies and the IDIC keys.
+__global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
+                          DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
+                          uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int q = ch.begin + threadIdx.x;
+    if (q >= ch.end) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    const int j = (int)order[q];
+    const double x = src.x[j], y = src.y[j], z = src.z[j];
+    dst.x[q] = x; dst.y[q] = y; dst.z[q] = z;
+    const double vx = src.vx[j], vy = src.vy[j], vz = src.vz[j];
+    dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
+    dst.ax[q] = src.ax[j]; dst.ay[q] = src.ay[j]; dst.az[q] = src.az[j];
+    dst.rho[q] = src.rho[j]; dst.p[q] = src.p[j]; dst.e[q] = src.e[j];
+    const double m = src.m[j], h = src.h[j];
+    dst.m[q] = m; dst.h[q] = h;
+    dst.ts[q] = src.ts[j];
+    const int ind = src.ind[j], pid = src.pid[j];
+    dst.ind[q] = ind; dst.pid[q] = pid;
+    const int gp = T.seg_begin[ch.species] + pid;
+    slot_of_pid[gp] = q;
+    ind_of_pid[gp] = ind;
+    // FP32 coordinates: offsets from the own cell origin (proper grid) or from
+    // the tube's reference point (reference grid)
+    float4 p4;
+    if (T.cellrel) {
+      int ix, iy, iz;
+      ds_proper_cell(T, x, y, z, ix, iy, iz);
+      p4.x = (float)(x - (T.ox + ix * T.wx));
+      p4.y = (float)(y - (T.oy + iy * T.wy));
+      p4.z = (float)(z - (T.oz + iz * T.wz));
+    } else {
+      p4.x = (float)(x - T.fx);
+      p4.y = (float)(y - T.fy);
+      p4.z = (float)(z - T.fz);
+    }
+    p4.w = (float)h;
+    pos32[q] = p4;
+    vm32[q] = make_float4((float)vx, (float)vy, (float)vz, (float)m);
+    const int ic = ds_idic_cell(T, x, y, z);
+    idic_local[q] = ic;
+    ikin[gp] = (uint32_t)(T.idic_base[ch.species] + (ic >= 0 ? ic : T.n_idic + 1));
+    ivin[gp] = (uint32_t)q;
+  }
+}
+
+// cell_start[k] = first sorted slot whose key is >= k, for k = 0..nkeys.
+__global__ void k_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q > n) return;
+  const long long prev = q > 0 ? (long long)skey[q - 1] : -1LL;
+  const long long cur = q < n ? (long long)skey[q] : (long long)nkeys;
+  for (long long k = prev + 1; k <= cur; k++) cell_start[k] = q;
+}
+
+// Index of the segment whose IDIC key range contains key (seg_key0 ascending).
+__device__ __forceinline__ int find_seg(const int *seg_key0, int nseg, int key) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (seg_key0[mid] <= key) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Per IDIC cell and species, sums in ascending particle index (the reference's
+// host loops, kernel.cu:2114-2123, 2137-2146, 2165-2174, 2294-2300).
+__global__ void k_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
+                              const int *seg_species, const int *seg_orphan, int nseg, DevState st,
+                              CellArrays ca) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint32_t key = ikey[q];
+  if (q > 0 && ikey[q - 1] == key) return;  // not the start of a run
+  const int sg = find_seg(seg_key0, nseg, (int)key);
+  if ((int)key == seg_orphan[sg]) return;    // outside the IDIC grid
+  const int s = seg_species[sg];
+  int cnt = 0;
+  double vx = 0.0, vy = 0.0, vz = 0.0, a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int r = q; r < n && ikey[r] == key; r++) {
+    const int j = (int)islot[r];
+    cnt = cnt + 1;
+    if (s > 0) a0 = a0 + st.ts[j];
+    vx = vx + st.vx[j];
+    vy = vy + st.vy[j];
+    vz = vz + st.vz[j];
+    if (s == 0) {
+      a0 = a0 + st.ax[j];
+      a1 = a1 + st.ay[j];
+      a2 = a2 + st.az[j];
+    }
+  }
+  ca.cnt[key] = cnt;
+  ca.vx[key] = vx; ca.vy[key] = vy; ca.vz[key] = vz;
+  ca.a0[key] = a0; ca.a1[key] = a1; ca.a2[key] = a2;
+}
+
+// One component of the per-cell implicit solve (kernel.cu:2310-2437); the
+// reference's two-species operation order when ref2, Sherman-Morrison for any
+// species count otherwise (the same algebra).  ND is a compile-time species
+// count so every array below lives in registers (fully unrolled loops).
+template <int ND>
+__device__ __forceinline__ void solve_comp(const double (&eps)[ND], const double (&t)[ND], double vg,
+                                           const double (&vd)[ND], double psi, double tau, bool ref2,
+                                           double &g_out, double (&d_out)[ND]) {
+  if constexpr (ND == 2) {
+    if (ref2) {
+      double y = vg, x1 = vg - vd[0], x2 = vg - vd[1];
+      y = y + eps[0] * vd[0] + eps[1] * vd[1];
+      double b1 = (t[0] + tau) / (eps[0] * tau);
+      double b2 = (t[1] + tau) / (eps[1] * tau);
+      double beta = 1.0;
+      beta = beta + 1.0 / b1 + 1.0 / b2;
+      double yn = y + tau * psi;
+      double x1n = -1.0 * b1 * beta * (x1 + tau * psi) / (b1 * b1);
+      x1n = x1n + (x1 + tau * psi) / (b1 * b1) + (x2 + tau * psi) / (b1 * b2);
+      x1n = x1n * (-1.0 * t[0]) / (tau * eps[0] * beta);
+      double x2n = -1.0 * b2 * beta * (x2 + tau * psi) / (b2 * b2);
+      x2n = x2n + (x1 + tau * psi) / (b2 * b1) + (x2 + tau * psi) / (b2 * b2);
+      x2n = x2n * (-1.0 * t[1]) / (tau * eps[1] * beta);
+      double tmp1 = 1.0;
+      tmp1 = tmp1 + eps[0] + eps[1];
+      double g = yn;
+      g = g + eps[0] * x1n;
+      double d1 = yn;
+      d1 = d1 + eps[1] * x2n;
+      d1 = d1 - (tmp1 - eps[0]) * x1n;
+      d1 = d1 / tmp1;
+      g = g + eps[1] * x2n;
+      double d2 = yn;
+      d2 = d2 + eps[0] * x1n;
+      d2 = d2 - (tmp1 - eps[1]) * x2n;
+      d2 = d2 / tmp1;
+      g = g / tmp1;
+      g_out = g;
+      d_out[0] = d1;
+      d_out[1] = d2;
+      return;
+    }
+  }
+  double b[ND], r[ND], xn[ND];
+  double y = vg, beta = 1.0, S = 0.0, E = 1.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    y = y + eps[k] * vd[k];
+    b[k] = (t[k] + tau) / (eps[k] * tau);
+    beta = beta + 1.0 / b[k];
+    r[k] = (vg - vd[k]) + tau * psi;
+    S = S + r[k] / b[k];
+    E = E + eps[k];
+  }
+  const double yn = y + tau * psi;
+  double g = yn;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    const double u = r[k] / b[k] - S / (b[k] * beta);
+    xn[k] = u * t[k] / (eps[k] * tau);
+    g = g + eps[k] * xn[k];
+  }
+  g = g / E;
+  g_out = g;
+#pragma unroll
+  for (int k = 0; k < ND; k++) d_out[k] = g - xn[k];
+}
+
+// Per (tube, IDIC cell): means (kernel.cu:2126-2190), eps (2192-2211),
+// Psi (2302-2309), solve (2310-2437).  Results are written at the cell's key
+// of each species: new velocities; for gas Psi; for dust the mean t_stop and eps.
+template <int ND>
+__device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double tau, CellArrays &ca) {
+  const int kg = T.idic_base[0] + c;
+  const int cg = ca.cnt[kg];
+  double vgx = 0.0, vgy = 0.0, vgz = 0.0, psx = 0.0, psy = 0.0, psz = 0.0;
+  if (cg > 0) {
+    vgx = ca.vx[kg] / cg; vgy = ca.vy[kg] / cg; vgz = ca.vz[kg] / cg;
+    psx = ca.a0[kg] / cg; psy = ca.a1[kg] / cg; psz = ca.a2[kg] / cg;
+  }
+  double eps[ND], tt[ND], vdx[ND], vdy[ND], vdz[ND];
+  const int c1 = ca.cnt[T.idic_base[1] + c];
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    const int kd = T.idic_base[k + 1] + c;
+    const int cd = ca.cnt[kd];
+    if (cd > 0) {
+      vdx[k] = ca.vx[kd] / cd; vdy[k] = ca.vy[kd] / cd; vdz[k] = ca.vz[kd] / cd;
+      tt[k] = ca.a0[kd] / cd;
+    } else {
+      vdx[k] = 0.0; vdy[k] = 0.0; vdz[k] = 0.0;
+      tt[k] = T.t_empty;
+    }
+    const int guard = (T.mode & M_REF_EPS_GUARD) ? c1 : cd;
+    eps[k] = ((cg > 0) && (guard > 0)) ? cd * T.mass_ratio[k] / cg : T.eps_empty[k];
+  }
+  const bool ref2 = (T.mode & M_REF_SOLVE2) != 0;
+  double gx, gy, gz, ox[ND], oy[ND], oz[ND];
+  solve_comp<ND>(eps, tt, vgx, vdx, psx, tau, ref2, gx, ox);
+  solve_comp<ND>(eps, tt, vgy, vdy, psy, tau, ref2, gy, oy);
+  solve_comp<ND>(eps, tt, vgz, vdz, psz, tau, ref2, gz, oz);
+  ca.nvx[kg] = gx; ca.nvy[kg] = gy; ca.nvz[kg] = gz;
+  ca.px[kg] = psx; ca.py[kg] = psy; ca.pz[kg] = psz;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    const int kd = T.idic_base[k + 1] + c;
+    ca.nvx[kd] = ox[k]; ca.nvy[kd] = oy[k]; ca.nvz[kd] = oz[k];
+    ca.px[kd] = tt[k];   // dust: mean t_stop
+    ca.py[kd] = eps[k];  // dust: eps
+  }
+}
+
+__global__ void k_idic_solve(const TubeDesc *tubes, const TubeState *tstate, const int *tube_cell0, int ntubes,
+                             int ncell_total, CellArrays ca) {
+  const int gc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gc >= ncell_total) return;
+  int lo = 0, hi = ntubes - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (tube_cell0[mid] <= gc) lo = mid; else hi = mid - 1;
+  }
+  const int t = lo;
+  if (!tstate[t].active) return;
+  const TubeDesc &T = tubes[t];
+  const int c = gc - tube_cell0[t];
+  const double tau = tstate[t].dt;
+  switch (T.n_dust) {
+    case 1: idic_solve_cell<1>(T, c, tau, ca); break;
+    case 2: idic_solve_cell<2>(T, c, tau, ca); break;
+    case 3: idic_solve_cell<3>(T, c, tau, ca); break;
+    default: idic_solve_cell<4>(T, c, tau, ca); break;
+  }
+}
+
+// V_dustKernel_IDIC / V_gasKernel_IDIC (IDIC.h:264-315), MoveKernel_IDIC
+// (IDIC.h:319-333, periodic wrap as an extension), EnergyKernel_IDIC (335-346).
+__global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, const Chunk *chunks, int nchunks,
+                             DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    if (i >= ch.end) continue;
+    if (!tstate[ch.tube].active) continue;
+    if (st.ind[i] != 0) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    const double tau = tstate[ch.tube].dt;
+    const int s = ch.species;
+    const int cell = idic_local[i];
+    double vx = st.vx[i], vy = st.vy[i], vz = st.vz[i];
+    if (cell < 0) {
+      atomicOr(flags, 1);  // DS_FLAG_IDIC_RANGE: left unrelaxed
+    } else if (s > 0) {
+      const int kg = T.idic_base[0] + cell, kd = T.idic_base[s] + cell;
+      const double ts = ca.px[kd];
+      vx = (vx / tau + ca.nvx[kg] / ts) / (1.0 / tau + 1.0 / ts);
+      vy = (vy / tau + ca.nvy[kg] / ts) / (1.0 / tau + 1.0 / ts);
+      vz = (vz / tau + ca.nvz[kg] / ts) / (1.0 / tau + 1.0 / ts);
+    } else {
+      const int kg = T.idic_base[0] + cell;
+      double tmp1 = 0.0, tmp_x = 0.0, tmp_y = 0.0, tmp_z = 0.0;
+      for (int k = 1; k <= T.n_dust; k++) {
+        const int kd = T.idic_base[k] + cell;
+        tmp1 = tmp1 + ca.py[kd] / ca.px[kd];
+      }
+      for (int k = 1; k <= T.n_dust; k++) {
+        const int kd = T.idic_base[k] + cell;
+        tmp_x = tmp_x + ca.py[kd] * ca.nvx[kd] / ca.px[kd];
+      }
+      for (int k = 1; k <= T.n_dust; k++) {
+        const int kd = T.idic_base[k] + cell;
+        tmp_y = tmp_y + ca.py[kd] * ca.nvy[kd] / ca.px[kd];
+      }
+      for (int k = 1; k <= T.n_dust; k++) {
+        const int kd = T.idic_base[k] + cell;
+        tmp_z = tmp_z + ca.py[kd] * ca.nvz[kd] / ca.px[kd];
+      }
+      const bool own = (T.mode & M_GAS_ACC_P) != 0;
+      const double ax = own ? st.ax[i] : ca.px[kg];
+      const double ay = own ? st.ay[i] : ca.py[kg];
+      const double az = own ? st.az[i] : ca.pz[kg];
+      vx = (vx / tau + tmp_x + ax) / (1.0 / tau + tmp1);
+      vy = (vy / tau + tmp_y + ay) / (1.0 / tau + tmp1);
+      vz = (vz / tau + tmp_z + az) / (1.0 / tau + tmp1);
+    }
+    st.vx[i] = vx; st.vy[i] = vy; st.vz[i] = vz;
+    double x = st.x[i] + vx * tau;
+    double y = st.y[i] + vy * tau;
+    double z = st.z[i] + vz * tau;
+    if (T.mode & M_PER_Y) {
+      if (y < T.oy) y = y + T.Ly;
+      else if (y >= T.ymax) y = y - T.Ly;
+    }
+    if (T.mode & M_PER_Z) {
+      if (z < T.oz) z = z + T.Lz;
+      else if (z >= T.zmax) z = z - T.Lz;
+    }
+    st.x[i] = x; st.y[i] = y; st.z[i] = z;
+    if (s == 0) st.e[i] = st.e[i] + edot[i] * tau;
+  }
+}
+
+// t_stop_Kernel_IDIC (IDIC.h:78-91): t = R / (sqrt(gam p/rho) rho) with the GAS
+// p, rho at the dust particle's own index (kernel.cu:2049); or constant.
+__global__ void k_tstop(const TubeDesc *tubes, const TubeState *tstate, const Chunk *chunks, int nchunks,
+                        DevState st, const int *gas_slot_of_pid, int *flags) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    if (i >= ch.end) continue;
+    if (!tstate[ch.tube].active) continue;
+    if (st.ind[i] != 0) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    const int k = ch.species - 1;
+    if (T.mode & M_TSTOP_CONST) {
+      st.ts[i] = T.t_stop_const[k];
+      continue;
+    }
+    const int q = st.pid[i];
+    const int ng = T.seg_end[0] - T.seg_begin[0];
+    if (q >= ng) {
+      atomicOr(flags, 2);
+      continue;
+    }
+    const int g = gas_slot_of_pid[T.seg_begin[0] + q];
+    const double p = st.p[g], rho = st.rho[g];
+    st.ts[i] = T.R_dust[k] / (sqrt(T.gam * p / rho) * rho);
+  }
+}
+
+// Step size per tube: fixed tau (kernel.cu:1931) or CFL number x min over
+// gas of h/(c + |v|), clipped to end exactly at T_end.
+__global__ void k_dt(const TubeDesc *tubes, TubeState *ts, int ntubes) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntubes) return;
+  if (!ts[t].active) return;
+  const TubeDesc &T = tubes[t];
+  double dt = T.tau;
+  if (T.mode & M_CFL) {
+    dt = T.cfl * __longlong_as_double((long long)ts[t].dtmin_bits);
+    if (ts[t].Tm + dt > T.t_end) dt = T.t_end - ts[t].Tm;
+  }
+  ts[t].dt = dt;
+}
+
+__global__ void k_step_end(TubeState *ts, int ntubes) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntubes) return;
+  if (!ts[t].active) return;
+  ts[t].Tm = ts[t].Tm + ts[t].dt;
+  ts[t].nstep = ts[t].nstep + 1;
+}
+
+// Conservation sums of one tube, deterministic: one block, fixed order.
+__global__ void k_conservation(const TubeDesc *tubes, int tube, DevState st, double *out) {
+  __shared__ double sh[6][256];
+  const TubeDesc &T = tubes[tube];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int ns = 1 + T.n_dust;
+  for (int s = 0; s < ns; s++)
+    for (int i = T.seg_begin[s] + threadIdx.x; i < T.seg_end[s]; i += blockDim.x) {
+      const double m = st.m[i];
+      acc[0] += m;
+      acc[1] += m * st.vx[i];
+      acc[2] += m * st.vy[i];
+      acc[3] += m * st.vz[i];
+      if (s == 0) acc[4] += m * st.e[i];
+      acc[5] += 0.5 * m * (st.vx[i] * st.vx[i] + st.vy[i] * st.vy[i] + st.vz[i] * st.vz[i]);
+    }
+  for (int k = 0; k < 6; k++) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int k = 0; k < 6; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; k++) out[k] = sh[k][0];
+}
+
+// Reference linked lists of one segment from the sorted order: head[c] = pid
+// of the first slot of cell c, next[pid] = pid of the following slot in the
+// same cell (kernel.cu:1937-1955), plus the raw key per pid.
+__global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState st, const int *cell_start,
+                              int *head, int *next, int *rawkey) {
+  const TubeDesc &T = tubes[tube];
+  const int b = T.seg_begin[s], e = T.seg_end[s];
+  const int q = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < e) {
+    const int pid = st.pid[q];
+    rawkey[pid] = ds_raw_key(T, st.x[q], st.y[q], st.z[q]);
+  }
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= T.ncells) {
+    const int kb = T.key_base[s];
+    const int j0 = cell_start[kb + c], j1 = cell_start[kb + c + 1];
+    head[c] = j0 < j1 ? st.pid[j0] : -1;
+    for (int j = j0; j < j1; j++) next[st.pid[j]] = (j + 1 < j1) ? st.pid[j + 1] : -1;
+  }
+}
+
+__global__ void k_fill(double *a, int n, double v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+__global__ void k_iota(int *a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = i;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launch wrappers (ds_kernels.cuh)
+// ---------------------------------------------------------------------------
+static inline int blocks_for(int n, int b) { return (n + b - 1) / b; }
+
+void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s) {
+  k_step_begin<<<blocks_for(ntubes, 64), 64, 0, s>>>(tubes, ts, ntubes);
+}
+void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
+                    uint32_t *vin, cudaStream_t s) {
+  if (nchunks) k_keys<<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
+}
+void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
+                       DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local, uint32_t *ikin,
+                       uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, cudaStream_t s) {
+  if (nchunks)
+    k_reorder<<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, src, dst, pos32, vm32, idic_local, ikin,
+                                           ivin, slot_of_pid, ind_of_pid);
+}
+void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s) {
+  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start);
+}
+void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
+                           const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
+                           cudaStream_t s) {
+  if (n) k_idic_reduce<<<blocks_for(n, 256), 256, 0, s>>>(ikey, islot, n, seg_key0, seg_species, seg_orphan, nseg,
+                                                          st, ca);
+}
+void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
+                          int ncell_total, CellArrays ca, cudaStream_t s) {
+  if (ncell_total) k_idic_solve<<<blocks_for(ncell_total, 128), 128, 0, s>>>(tubes, ts, tube_cell0, ntubes,
+                                                                             ncell_total, ca);
+}
+void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
+                          DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags,
+                          cudaStream_t s) {
+  if (nchunks) k_relax_move<<<nchunks, DS_CHUNK, 0, s>>>(tubes, ts, chunks, nchunks, st, idic_local, edot, ca, flags);
+}
+void ds_launch_tstop(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
+                     const int *gas_slot_of_pid, int *flags, cudaStream_t s) {
+  if (nchunks) k_tstop<<<nchunks, DS_CHUNK, 0, s>>>(tubes, ts, chunks, nchunks, st, gas_slot_of_pid, flags);
+}
+void ds_launch_dt(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s) {
+  k_dt<<<blocks_for(ntubes, 64), 64, 0, s>>>(tubes, ts, ntubes);
+}
+void ds_launch_step_end(TubeState *ts, int ntubes, cudaStream_t s) {
+  k_step_end<<<blocks_for(ntubes, 64), 64, 0, s>>>(ts, ntubes);
+}
+void ds_launch_conservation(const TubeDesc *tubes, int tube, DevState st, double *out, cudaStream_t s) {
+  k_conservation<<<1, 256, 0, s>>>(tubes, tube, st, out);
+}
+void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nseg_particles, int ncells,
+                           DevState st, const int *cell_start, int *head, int *next, int *rawkey,
+                           cudaStream_t s) {
+  int n = nseg_particles > ncells + 1 ? nseg_particles : ncells + 1;
+  k_debug_lists<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, species, st, cell_start, head, next, rawkey);
+}
+void ds_launch_fill(double *a, int n, double v, cudaStream_t s) {
+  if (n > 0) k_fill<<<blocks_for(n, 256), 256, 0, s>>>(a, n, v);
+}
+void ds_launch_iota(int *a, int n, cudaStream_t s) {
+  if (n > 0) k_iota<<<blocks_for(n, 256), 256, 0, s>>>(a, n);
+}

@@ -1,0 +1,53 @@
+// ds_kernels.cuh -- launch wrappers of the step kernels (ds_cells.cu,
+// ds_sweep64.cu, ds_sweep32.cu).  Every wrapper only enqueues work on the
+// given stream, so a whole step can be captured into a CUDA graph.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ds_common.cuh"
+
+#define DS_CHUNK 128  // particles per chunk = threads per block of the per-particle kernels
+
+// Per-key arrays of the IDIC cells (one key per tube, species and cell).
+struct CellArrays {
+  int *cnt;
+  double *vx, *vy, *vz;     // velocity sums
+  double *a0, *a1, *a2;     // gas: sums of A; dust: a0 = sum of t_stop
+  double *nvx, *nvy, *nvz;  // solved cell velocities
+  double *px, *py, *pz;     // gas: Psi; dust: px = mean t_stop, py = eps
+};
+
+void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
+void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
+                    uint32_t *vin, cudaStream_t s);
+void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
+                       DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local, uint32_t *ikin,
+                       uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, cudaStream_t s);
+void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s);
+void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
+                           const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
+                           cudaStream_t s);
+void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
+                          int ncell_total, CellArrays ca, cudaStream_t s);
+void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
+                          DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags,
+                          cudaStream_t s);
+void ds_launch_tstop(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
+                     const int *gas_slot_of_pid, int *flags, cudaStream_t s);
+void ds_launch_dt(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
+void ds_launch_step_end(TubeState *ts, int ntubes, cudaStream_t s);
+void ds_launch_conservation(const TubeDesc *tubes, int tube, DevState st, double *out, cudaStream_t s);
+void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nseg_particles, int ncells,
+                           DevState st, const int *cell_start, int *head, int *next, int *rawkey, cudaStream_t s);
+
+void ds_launch_fill(double *a, int n, double v, cudaStream_t s);
+void ds_launch_iota(int *a, int n, cudaStream_t s);
+
+// Sweeps.  what: 0 = gas density + EOS (+ derived c, p/rho^2, CFL minimum),
+// 1 = dust self-density, 2 = counts only (parity hook, any species).
+void ds_launch_density64(const SweepArgs &a, bool hpp, bool proper, int what, cudaStream_t s);
+void ds_launch_force64(const SweepArgs &a, bool hpp, bool proper, cudaStream_t s);
+void ds_launch_counts64(const SweepArgs &a, bool hpp, bool proper, cudaStream_t s);
+void ds_launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s);
+void ds_launch_force32(const SweepArgs &a, bool hpp, cudaStream_t s);

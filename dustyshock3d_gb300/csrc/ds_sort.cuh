@@ -1,0 +1,15 @@
+// ds_sort.cuh -- stable LSD radix sort of (key, value) pairs (ds_sort.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+// 32-bit words of scratch the sort of n pairs needs.
+size_t ds_radix_scratch_words(int n);
+int ds_radix_passes(int key_bits);
+
+// Sorts the low key_bits of keys[0..n) with their vals, stably.  The sorted
+// pairs end in (keys, vals) or, when *result_in_alt, in (keys_alt, vals_alt).
+// Launch-only: capturable into a CUDA graph.
+cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, int n,
+                          int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt);

@@ -1,0 +1,224 @@
+// ds_sweep32.cu -- FP32 neighbour sweeps with Kahan-compensated sums.
+//
+// Same traversal as ds_sweep64.cu (27 cells in the reference's order, one
+// thread per particle), but every per-pair quantity is FP32: positions are FP32
+// offsets from the particle's own cell origin (proper grid; a neighbour cell's
+// offsets are shifted by whole cell widths, which also applies the periodic
+// image), velocities/masses come from packed float4 copies, and each sum is
+// Kahan-compensated.  The kernel normalisation 1/(pi h^3) is applied once per
+// particle in FP64.  State, the IDIC exchange and the conservation sums stay
+// FP64 (ds_cells.cu).  GB300 issues FP32 at ~64x its FP64 rate, which is what
+// this path is for; its error against the FP64 path is measured, not assumed.
+#include <cuda_runtime.h>
+
+#include "ds_common.cuh"
+#include "ds_kernels.cuh"
+
+namespace {
+
+struct Kahan {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// M4 shape without normalisation, q = r/h >= 0 (kernel.cu:18-20)
+__device__ __forceinline__ float w_shape(float q) {
+  if (q < 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
+  if (q <= 2.0f) {
+    const float t = 2.0f - q;
+    return 0.25f * t * t * t;
+  }
+  return 0.0f;
+}
+
+// derivative shape, q >= 0 (kernel.cu:34-36)
+__device__ __forceinline__ float dw_shape(float q) {
+  if (q <= 1.0f) return -3.0f * q + 2.25f * q * q;
+  if (q <= 2.0f) {
+    const float t = 2.0f - q;
+    return -0.75f * t * t;
+  }
+  return 0.0f;
+}
+
+__device__ __forceinline__ void cell_shift(const TubeDesc &T, int o, double shy, double shz, float &sx, float &sy,
+                                           float &sz) {
+  if (T.cellrel) {
+    const int k = o / 9 - 1, l = (o / 3) % 3 - 1, g = o % 3 - 1;
+    sx = (float)(k * T.wx);
+    sy = (float)(l * T.wy);
+    sz = (float)(g * T.wz);
+  } else {
+    sx = 0.0f;
+    sy = (float)shy;
+    sz = (float)shz;
+  }
+}
+
+template <bool HPP, int WHAT>
+__global__ void __launch_bounds__(DS_CHUNK) k_density32(SweepArgs a) {
+  const float c_pi = 1.0f / 3.14159265f;
+  (void)c_pi;
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    const Chunk ch = a.chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    if (i >= ch.end) continue;
+    if (!a.tstate[ch.tube].active) continue;
+    const TubeDesc &T = a.tubes[ch.tube];
+    const int s = ch.species;
+    const int ind = a.st.ind[i];
+    const bool upd = ind == 0;
+    bool zero = upd;
+    if (WHAT == 1 && (T.mode & M_REF_COUPLING)) {
+      const int q = a.st.pid[i];
+      const int ng = T.seg_end[0] - T.seg_begin[0];
+      zero = q < ng && a.gas_ind_pid[T.seg_begin[0] + q] == 0;
+    }
+    double rho = a.st.rho[i];
+    if (zero) rho = 0.0;
+    if (upd) {
+      const double xi = a.st.x[i], yi = a.st.y[i], zi = a.st.z[i];
+      const double hd = HPP ? a.st.h[i] : T.h;
+      const float4 pi = a.pos32[i];
+      const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
+      Stencil S;
+      ds_stencil_init(T, xi, yi, zi, S);
+      const int kb = T.key_base[s];
+      Kahan sum;
+      for (int o = 0; o < 27; o++) {
+        double shy, shz;
+        const int cell = ds_stencil_cell(T, S, o, shy, shz);
+        if (cell < 0) continue;
+        float sx, sy, sz;
+        cell_shift(T, o, shy, shz, sx, sy, sz);
+        const int j1 = a.cell_start[kb + cell + 1];
+        for (int j = a.cell_start[kb + cell]; j < j1; j++) {
+          const float4 pj = a.pos32[j];
+          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 >= cut2) continue;
+          sum.add(a.vm32[j].w * w_shape(sqrtf(r2) * inv_h));
+        }
+      }
+      const double norm = ((double)1 / (DS_PI_REF)) / (hd * hd * hd);
+      rho = rho + norm * sum.value();
+    }
+    if (zero || upd) a.st.rho[i] = rho;
+    if (WHAT == 0) {
+      double p = a.st.p[i];
+      if (upd) {
+        p = ds_eq_state(rho, a.st.e[i], T.type_of_state, T.gam, T.cs);
+        a.st.p[i] = p;
+      }
+      const double cs = sqrt(T.gam * p / rho);
+      const double pt = p / (rho * rho);
+      a.cs64[i] = cs;
+      a.pt64[i] = pt;
+      a.hyd32[i] = make_float4((float)cs, (float)pt, (float)rho, 0.0f);
+      if (upd && (T.mode & M_CFL)) {
+        const double vx = a.st.vx[i], vy = a.st.vy[i], vz = a.st.vz[i];
+        const double v = sqrt(vx * vx + vy * vy + vz * vz);
+        const double hh = HPP ? a.st.h[i] : T.h;
+        const double dt = hh / (cs + v);
+        atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong(dt));
+      }
+    }
+  }
+}
+
+template <bool HPP>
+__global__ void __launch_bounds__(DS_CHUNK) k_force32(SweepArgs a) {
+  const float c_pi = (float)(1.0 / 3.14159265);
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    const Chunk ch = a.chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    if (i >= ch.end) continue;
+    if (!a.tstate[ch.tube].active) continue;
+    if (a.st.ind[i] != 0) continue;
+    const TubeDesc &T = a.tubes[ch.tube];
+    const int s = ch.species;
+    const double xi = a.st.x[i], yi = a.st.y[i], zi = a.st.z[i];
+    const float4 pi = a.pos32[i];
+    const float4 vmi = a.vm32[i];
+    const float4 hyi = a.hyd32[i];
+    const float hi = HPP ? pi.w : (float)T.h;
+    const float inv_hi = 1.0f / hi;
+    const float ni = c_pi * inv_hi * inv_hi * inv_hi * inv_hi;
+    const float mi = vmi.w, rhoi = hyi.z, pti = hyi.y, csi = hyi.x;
+    const float mpi = (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i]));
+    const float alpha = (float)T.alpha, beta = (float)T.beta, eps = (float)T.eps;
+    Kahan Ax, Ay, Az, et;
+    Stencil S;
+    ds_stencil_init(T, xi, yi, zi, S);
+    const int kb = T.key_base[s];
+    for (int o = 0; o < 27; o++) {
+      double shy, shz;
+      const int cell = ds_stencil_cell(T, S, o, shy, shz);
+      if (cell < 0) continue;
+      float sx, sy, sz;
+      cell_shift(T, o, shy, shz, sx, sy, sz);
+      const int j1 = a.cell_start[kb + cell + 1];
+      for (int j = a.cell_start[kb + cell]; j < j1; j++) {
+        const float4 pj = a.pos32[j];
+        const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float hj = HPP ? pj.w : hi;
+        const float hc = HPP ? fmaxf(hi, hj) : hi;
+        if (!(r2 < 4.0f * hc * hc) || !(r2 > 0.0f)) continue;
+        const float dist = sqrtf(r2);
+        const float inv_d = 1.0f / dist;
+        const float4 vmj = a.vm32[j];
+        const float4 hyj = a.hyd32[j];
+        const float hh = HPP ? 0.5f * (hi + hj) : hi;
+        const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
+        float F = 0.0f;
+        if (nu < 0.0f) {
+          const float Cnu = 0.5f * (csi + hyj.x);
+          const float mu = hh * nu / (r2 + eps * hh * hh);
+          F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
+        }
+        float dWr = ni * dw_shape(dist * inv_hi);
+        if (HPP) {
+          const float inv_hj = 1.0f / hj;
+          const float nj = c_pi * inv_hj * inv_hj * inv_hj * inv_hj;
+          dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
+        }
+        const float gd = dWr * inv_d;
+        et.add((mpi + mi * F * 0.5f) * nu * gd);
+        const float A = vmj.w * (pti + hyj.y + F) * gd;
+        Ax.add(dx * A);
+        Ay.add(dy * A);
+        Az.add(dz * A);
+      }
+    }
+    a.st.ax[i] = Ax.value();
+    a.st.ay[i] = Ay.value();
+    a.st.az[i] = Az.value();
+    a.edot[i] = et.value();
+  }
+}
+
+}  // namespace
+
+void ds_launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
+  if (!a.nchunks) return;
+  if (what == 0) {
+    if (hpp) k_density32<true, 0><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+    else k_density32<false, 0><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+  } else {
+    if (hpp) k_density32<true, 1><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+    else k_density32<false, 1><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+  }
+}
+
+void ds_launch_force32(const SweepArgs &a, bool hpp, cudaStream_t s) {
+  if (!a.nchunks) return;
+  if (hpp) k_force32<true><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+  else k_force32<false><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+}

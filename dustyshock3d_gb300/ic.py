@@ -129,7 +129,7 @@ def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0
                    gamma: float = 1.4, h_factor: float = 1.3, x_range=(-0.5, 0.5), wall: float = 2.5,
                    t_end: float = 0.2, cfl: float = 0.3, alpha: float = 1.0, beta: float = 2.0,
                    av_eps: float = 0.01, idic_cells_per_right_spacing: float = 2.0,
-                   fixed_tau: float = None) -> Tuple[Params, List[Species]]:
+                   fixed_tau: float = None, lattice_offset: float = 0.25) -> Tuple[Params, List[Species]]:
     """Dusty Sod tube on [x0, x1] x [0, Ly] x [0, Lz], periodic in y and z.
 
     The left state sits on a cubic lattice of spacing ``dx_left``; the right
@@ -139,6 +139,13 @@ def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0
     offset by half a spacing in x, y and z, with mass eps x the gas mass.
     Particles within ``wall`` smoothing lengths of either x end are frozen
     (Ind = 1), like the reference's border particles (kernel.cu:1396, 1441).
+
+    Gas sites sit at (i + lattice_offset) spacings from the lower faces and
+    dust sites half a spacing further.  With the default 0.25 no particle
+    starts on a face of the IDIC grid (width 2 right spacings = 4 left
+    spacings, origin at the lower box corner): a lattice on the faces would
+    put whole columns of dust exactly on them, and rounding-level motion would
+    then move a column between cells and change the cells' eps at once.
     """
     Lz = Ly if Lz is None else Lz
     x0, x1 = x_range
@@ -156,9 +163,9 @@ def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0
         hloc = h_factor * (dx * dy * dz) ** (1.0 / 3.0)
         i, j, k = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64),
                               np.arange(nz, dtype=np.float64), indexing="ij")
-        gx = xa + (i.ravel() + 0.5) * dx
-        gy = (j.ravel() + 0.5) * dy
-        gz = (k.ravel() + 0.5) * dz
+        gx = xa + (i.ravel() + lattice_offset) * dx
+        gy = (j.ravel() + lattice_offset) * dy
+        gz = (k.ravel() + lattice_offset) * dz
         # dust: offset by half a spacing (y, z wrap onto the periodic lattice)
         dxp = gx + 0.5 * dx
         dyp = np.mod(gy + 0.5 * dy, Ly)

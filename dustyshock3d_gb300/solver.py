@@ -1,0 +1,174 @@
+"""Host-side mirror of the reference's step driver over the C ABI.
+
+``Solver`` plays the part of the reference's ``main`` between set-up and output
+(kernel.cu:1929-2566): it uploads the SoA particle arrays once, advances them on
+the device and downloads them at output times.  A ``Solver`` built from several
+``Params`` advances that many independent tubes together (batched launches, one
+CUDA graph per step).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Sequence
+
+import numpy as np
+
+from . import _lib
+from .params import Params
+from .species import Species
+
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_DP)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_IP)
+
+
+def _f64(a, n):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    assert a.shape == (n,), (a.shape, n)
+    return a
+
+
+class Solver:
+    def __init__(self, params):
+        self.L = _lib.load()
+        plist: List[Params] = list(params) if isinstance(params, (list, tuple)) else [params]
+        self.params = plist
+        arr = (_lib.DsParams * len(plist))(*[_lib.params_to_c(p) for p in plist])
+        self._cparams = arr
+        ctx = ctypes.c_void_p()
+        st = self.L.ds_create_batch(len(plist), arr, ctypes.byref(ctx))
+        _lib.check(self.L, None, st, "ds_create_batch")
+        self.ctx = ctx
+        self.n = [[None] * (1 + p.n_dust) for p in plist]
+
+    # -- upload -------------------------------------------------------------
+    def set_species(self, tube: int, s: int, sp: Species):
+        n = sp.n
+        g = lambda f: _f64(getattr(sp, f), n)  # noqa: E731
+        ind = np.ascontiguousarray(sp.ind if sp.ind is not None else np.zeros(n, np.int32), dtype=np.int32)
+        keep = {f: g(f) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h", "ts")}
+        if s == 0:
+            st = self.L.ds_set_gas(self.ctx, tube, n, *[_dp(keep[f]) for f in
+                                                        ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho",
+                                                         "p", "e", "m", "h")], _ip(ind))
+        else:
+            st = self.L.ds_set_dust(self.ctx, tube, s, n, *[_dp(keep[f]) for f in
+                                                            ("x", "y", "z", "vx", "vy", "vz", "rho", "m", "ts",
+                                                             "h")], _ip(ind))
+        _lib.check(self.L, self.ctx, st, f"set species {s} of tube {tube}")
+        self.n[tube][s] = n
+
+    def set_tube(self, tube: int, species: Sequence[Species]):
+        for s, sp in enumerate(species):
+            self.set_species(tube, s, sp.copy().fill_missing())
+
+    # -- stepping -----------------------------------------------------------
+    def step(self, n: int = 1):
+        _lib.check(self.L, self.ctx, self.L.ds_step(self.ctx, int(n)), "ds_step")
+
+    def step_async(self, n: int = 1):
+        _lib.check(self.L, self.ctx, self.L.ds_step_async(self.ctx, int(n)), "ds_step_async")
+
+    def synchronize(self):
+        _lib.check(self.L, self.ctx, self.L.ds_synchronize(self.ctx), "ds_synchronize")
+
+    def step_timed(self, n: int = 1):
+        tot = ctypes.c_float(0)
+        ph = (ctypes.c_float * _lib.DS_NPHASE)()
+        _lib.check(self.L, self.ctx, self.L.ds_step_timed(self.ctx, int(n), ctypes.byref(tot), ph), "ds_step_timed")
+        return tot.value, list(ph)
+
+    # -- download -----------------------------------------------------------
+    def get_species(self, tube: int, s: int, template: Species = None) -> Species:
+        n = self.n[tube][s]
+        out = {f: np.empty(n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "rho")}
+        ind = np.empty(n, np.int32)
+        if s == 0:
+            for f in ("ax", "ay", "az", "p", "e"):
+                out[f] = np.empty(n, np.float64)
+            st = self.L.ds_get_gas(self.ctx, tube, *[_dp(out[f]) for f in
+                                                     ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p",
+                                                      "e")], _ip(ind))
+        else:
+            out["ts"] = np.empty(n, np.float64)
+            st = self.L.ds_get_dust(self.ctx, tube, s, *[_dp(out[f]) for f in
+                                                         ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")], _ip(ind))
+        _lib.check(self.L, self.ctx, st, f"get species {s} of tube {tube}")
+        sp = Species(ind=ind, **out)
+        if template is not None:
+            sp.m = template.m.copy()
+            sp.h = None if template.h is None else template.h.copy()
+        return sp
+
+    def time(self, tube: int = 0):
+        Tm, dt = ctypes.c_double(), ctypes.c_double()
+        ns = ctypes.c_longlong()
+        _lib.check(self.L, self.ctx, self.L.ds_get_time(self.ctx, tube, ctypes.byref(Tm), ctypes.byref(dt),
+                                                        ctypes.byref(ns)), "ds_get_time")
+        return Tm.value, dt.value, ns.value
+
+    def debug_cells(self, tube: int, s: int):
+        n = self.n[tube][s]
+        nc = ctypes.c_int(0)
+        # first call for ncells
+        key = np.empty(max(n, 1), np.int32)
+        nxt = np.empty(max(n, 1), np.int32)
+        cand = np.empty(max(n, 1), np.int32)
+        nnb = np.empty(max(n, 1), np.int32)
+        _lib.check(self.L, self.ctx, self.L.ds_debug_cells(self.ctx, tube, s, None, None, None, None, None,
+                                                           ctypes.byref(nc)), "ds_debug_cells")
+        head = np.empty(nc.value + 1, np.int32)
+        _lib.check(self.L, self.ctx, self.L.ds_debug_cells(self.ctx, tube, s, _ip(key), _ip(head), _ip(nxt),
+                                                           _ip(cand), _ip(nnb), ctypes.byref(nc)), "ds_debug_cells")
+        return dict(cell_key=key[:n], head=head, next=nxt[:n], ncand=cand[:n], nnb=nnb[:n], ncells=nc.value)
+
+    def debug_idic(self, tube: int, s: int):
+        n = ctypes.c_int(0)
+        _lib.check(self.L, self.ctx, self.L.ds_debug_idic(self.ctx, tube, s, None, None, ctypes.byref(n)),
+                   "ds_debug_idic")
+        cnt = np.empty(n.value, np.int32)
+        cells = np.empty((12, n.value), np.float64)
+        _lib.check(self.L, self.ctx, self.L.ds_debug_idic(self.ctx, tube, s, _ip(cnt), _dp(cells), ctypes.byref(n)),
+                   "ds_debug_idic")
+        return cnt, cells
+
+    def conservation(self, tube: int = 0):
+        out = np.zeros(6, np.float64)
+        _lib.check(self.L, self.ctx, self.L.ds_conservation(self.ctx, tube, _dp(out)), "ds_conservation")
+        return out
+
+    def kernels_per_step(self):
+        k = ctypes.c_int(0)
+        _lib.check(self.L, self.ctx, self.L.ds_kernels_per_step(self.ctx, ctypes.byref(k)), "ds_kernels_per_step")
+        return k.value
+
+    def memory_bytes(self):
+        b = ctypes.c_longlong(0)
+        _lib.check(self.L, self.ctx, self.L.ds_memory_bytes(self.ctx, ctypes.byref(b)), "ds_memory_bytes")
+        return b.value
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.ds_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -1,0 +1,208 @@
+/*
+ * dustyshock3d_gb300.h -- C ABI of the GB300 (sm_103a) per-step dusty-gas
+ * SPH + IDIC solver.
+ *
+ * Drop-in for the inline step loop of the reference program
+ * (kernel.cu:1929-2523 with the IDIC.h kernels).  The reference's host driver
+ * keeps its config parser (kernel.cu:1705-1742), initial conditions
+ * (kernel.cu:1391) and snapshot output (kernel.cu:2528-2564); in between it
+ * uploads its SoA FP64 arrays once (data.h:19-20, 49-55), calls ds_step for
+ * the time loop and downloads at output times.  Nothing here includes data.h
+ * (it defines globals).
+ *
+ * Conventions
+ *  - every call returns a ds_status; nothing aborts, traps or exits;
+ *  - host arrays are caller-owned and are read or written only during the
+ *    call; device memory is owned by the context;
+ *  - particle arrays are in the caller's index order (index p = 0..n-1, the
+ *    reference's 0..Pm); the library sorts internally and restores the order
+ *    on download;
+ *  - one context per host thread; a context uses the current CUDA device at
+ *    ds_create time and its own stream.
+ */
+#ifndef DUSTYSHOCK3D_GB300_H
+#define DUSTYSHOCK3D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DS_MAX_DUST 4
+#define DS_NPHASE 4 /* timed phases per step, see ds_phase_times */
+
+typedef enum ds_status {
+  DS_OK = 0,
+  DS_ERR_ARG = 1,      /* invalid argument (null pointer, bad size, bad species) */
+  DS_ERR_CUDA = 2,     /* a CUDA runtime call failed; see ds_last_error          */
+  DS_ERR_STATE = 3,    /* call out of order (e.g. step before particles are set) */
+  DS_ERR_NOMEM = 4,    /* device allocation failed                                */
+  DS_ERR_DEVICE = 5,   /* a kernel raised a sticky device-side flag               */
+  DS_ERR_UNSUPPORTED = 6
+} ds_status;
+
+/* Device-side flags (sticky per context, read with ds_last_error). */
+#define DS_FLAG_IDIC_RANGE 0x1 /* a particle's IDIC cell index was outside the grid
+                                  (the reference writes out of bounds there,
+                                  kernel.cu:2116-2117); it was left unrelaxed   */
+#define DS_FLAG_PID_RANGE 0x2  /* dust index beyond the gas count in the index-
+                                  coupled stopping time (IDIC.h:86)             */
+
+/* Mode bits (ds_params.mode).  0 = the reference's own step. */
+#define DS_MODE_PERIODIC_Y 0x0001
+#define DS_MODE_PERIODIC_Z 0x0002
+#define DS_MODE_H_PER_PARTICLE 0x0004  /* h_i per particle; symmetrised gradient  */
+#define DS_MODE_TSTOP_CONST 0x0008     /* constant stopping time per species      */
+#define DS_MODE_GAS_ACCEL_PARTICLE 0x0010 /* gas relaxes with its own A_i, not Psi */
+#define DS_MODE_REF_INDEX_COUPLING 0x0020 /* dust rho zeroed by gas Ind[p] (IDIC.h:8) */
+#define DS_MODE_REF_EPS_GUARD 0x0040   /* all eps guards test species-1 count (kernel.cu:2203) */
+#define DS_MODE_REF_SOLVE2 0x0080      /* 2-species solve in the reference's order */
+#define DS_MODE_CFL 0x0100             /* CFL step instead of fixed tau           */
+#define DS_MODE_DUST_RHO 0x0200        /* dust self-density every step            */
+#define DS_MODE_GRID_PROPER 0x0400     /* cell key stride nx (reference: Cnx)     */
+#define DS_MODE_IDIC_PROPER 0x0800     /* IDIC key stride nx (reference: Nax)     */
+#define DS_MODE_REFERENCE (DS_MODE_REF_INDEX_COUPLING | DS_MODE_REF_EPS_GUARD | \
+                           DS_MODE_REF_SOLVE2 | DS_MODE_DUST_RHO)
+
+#define DS_PRECISION_FP64 0 /* FP64 everywhere, reference operation order */
+#define DS_PRECISION_FP32 1 /* FP32 neighbour sums (Kahan), cell-relative FP32
+                               positions; FP64 state, IDIC exchange, sums   */
+
+/* Run parameters: Init.txt lines 2-18 (kernel.cu:1707-1723), the constants the
+ * reference hard-codes, and the extensions.  Fill with ds_params_init. */
+typedef struct ds_params {
+  double X_min, X_max, Y_min, Y_max, Z_min, Z_max; /* Init.txt 2-7              */
+  int Type_of_state;                               /* Init.txt 8 (0: p=rho e(g-1), 1: c^2 rho) */
+  int Maximum_particle;                            /* Init.txt 9                */
+  double Particle_on_length;                       /* Init.txt 10 (IC only)     */
+  double h;                                        /* Init.txt 11               */
+  double Coeff_h_dust_cell;                        /* Init.txt 12               */
+  double tau, T_end, T_out;                        /* Init.txt 13-15            */
+  double alpha, beta, eps;                         /* Init.txt 16-18            */
+  double Gam_g;              /* data.h:7, 1.4                                    */
+  double Speed_of_sound_gas; /* kernel.cu:1744, 1.0                              */
+  int n_dust;                /* dust species, 1..DS_MAX_DUST (reference: 2)      */
+  int mode;                  /* DS_MODE_* bits                                   */
+  int precision;             /* DS_PRECISION_*                                   */
+  int reserved0;
+  double cell_w;             /* neighbour cell width; 0 -> 2h (kernel.cu:1773)   */
+  double idic_w;             /* IDIC cell width; 0 -> Coeff_h_dust_cell*h (kernel.cu:1577) */
+  double cfl;                /* CFL number (DS_MODE_CFL)                          */
+  double t_empty;            /* mean t_stop of a cell without dust (kernel.cu:2160) */
+  double mass_ratio[DS_MAX_DUST];   /* mas_gas_dust_k (kernel.cu:1499-1502)       */
+  double R_dust[DS_MAX_DUST];       /* R_dust_k for t_stop = R/(c_s rho) (IDIC.h:86) */
+  double t_stop_const[DS_MAX_DUST]; /* DS_MODE_TSTOP_CONST                        */
+  double eps_empty[DS_MAX_DUST];    /* eps of a cell failing its guard (kernel.cu:2200, 2209) */
+} ds_params;
+
+typedef struct ds_ctx ds_ctx;
+
+/* Fills p with the reference's Init.txt values and constants (DS_MODE_REFERENCE). */
+ds_status ds_params_init(ds_params *p);
+
+/* Parses an Init.txt the way the reference's main does (kernel.cu:1705-1723):
+ * title line, then 17 positional values, trailing comments ignored. */
+ds_status ds_params_read_init_txt(const char *path, ds_params *p);
+
+/* One tube (the reference's single domain).  Replaces the reference's device
+ * allocation and upload block (kernel.cu:1793-1926). */
+ds_status ds_create(const ds_params *p, ds_ctx **out);
+
+/* ntubes independent tubes advanced together (batched launches). */
+ds_status ds_create_batch(int ntubes, const ds_params *p, ds_ctx **out);
+
+/* Gas arrays of one tube, reference layout (data.h:19-20).  h may be NULL
+ * (then h = params.h for every particle); ax, ay, az may be NULL (zero). */
+ds_status ds_set_gas(ds_ctx *c, int tube, int n, const double *x, const double *y, const double *z,
+                     const double *vx, const double *vy, const double *vz, const double *ax,
+                     const double *ay, const double *az, const double *rho, const double *p,
+                     const double *e, const double *mas, const double *h, const int *ind);
+
+/* Dust species k (1..n_dust) of one tube, reference layout (data.h:49-55). */
+ds_status ds_set_dust(ds_ctx *c, int tube, int species, int n, const double *x, const double *y,
+                      const double *z, const double *vx, const double *vy, const double *vz,
+                      const double *rho, const double *mas, const double *t_stop, const double *h,
+                      const int *ind);
+
+/* Single-tube names the reference's host driver binds (tube 0). */
+ds_status ds_upload_gas(ds_ctx *c, int n, const double *x, const double *y, const double *z,
+                        const double *vx, const double *vy, const double *vz, const double *ax,
+                        const double *ay, const double *az, const double *rho, const double *p,
+                        const double *e, const double *mas, const double *h, const int *ind);
+ds_status ds_upload_dust(ds_ctx *c, int species, int n, const double *x, const double *y,
+                         const double *z, const double *vx, const double *vy, const double *vz,
+                         const double *rho, const double *mas, const double *t_stop,
+                         const double *h, const int *ind);
+
+/* Advances every tube whose time is below its T_end by up to nsteps steps
+ * (the body of the reference's do-while loop, kernel.cu:1929-2566).  State
+ * stays on the device; returns after the device has finished. */
+ds_status ds_step(ds_ctx *c, int nsteps);
+
+/* Same, without waiting for the device (errors surface at the next sync). */
+ds_status ds_step_async(ds_ctx *c, int nsteps);
+ds_status ds_synchronize(ds_ctx *c);
+
+/* Downloads in the caller's index order; any pointer may be NULL (skipped). */
+ds_status ds_get_gas(ds_ctx *c, int tube, double *x, double *y, double *z, double *vx, double *vy,
+                     double *vz, double *ax, double *ay, double *az, double *rho, double *p,
+                     double *e, int *ind);
+ds_status ds_get_dust(ds_ctx *c, int tube, int species, double *x, double *y, double *z, double *vx,
+                      double *vy, double *vz, double *rho, double *t_stop, int *ind);
+ds_status ds_download_gas(ds_ctx *c, double *x, double *y, double *z, double *vx, double *vy,
+                          double *vz, double *ax, double *ay, double *az, double *rho, double *p,
+                          double *e, int *ind);
+ds_status ds_download_dust(ds_ctx *c, int species, double *x, double *y, double *z, double *vx,
+                           double *vy, double *vz, double *rho, double *t_stop, int *ind);
+
+/* Simulation time Tm, last step size and steps taken of one tube. */
+ds_status ds_get_time(ds_ctx *c, int tube, double *Tm, double *dt_last, long long *nsteps);
+
+/* Parity hook: for the particles' CURRENT positions, the raw cell key of each
+ * particle (kernel.cu:1949), the reference's linked lists (head[ncells+1] =
+ * Cell_*, next[n] = Nn_*, kernel.cu:1937-1955) reconstructed from the sorted
+ * order, and per particle the candidates visited over the 27 offsets and the
+ * number with 0 < r < 2h (IDIC.h:219-220), from the production sweep.  Any
+ * pointer may be NULL.  *ncells receives Number_of_fihd_cells. */
+ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *head, int *next,
+                         int *ncand, int *nnb, int *ncells);
+
+/* Parity hook: the IDIC cell arrays of one species as left by the last step
+ * (cells 0..Number_of_average_cell, kernel.cu:2060-2437): count[n] and
+ * cells[12][n] = sums of Vx, Vy, Vz; sums of Ax, Ay, Az (gas) or of t_stop
+ * (dust, first row); solved Vx, Vy, Vz; Psi x, y, z (gas) or mean t_stop and
+ * eps (dust).  *ncells receives n.  Any pointer may be NULL. */
+ds_status ds_debug_idic(ds_ctx *c, int tube, int species, int *count, double *cells, int *ncells);
+
+/* Global FP64 sums of one tube: out[0] mass, out[1..3] momentum, out[4] gas
+ * internal energy sum m e, out[5] kinetic energy (all species). */
+ds_status ds_conservation(ds_ctx *c, int tube, double *out6);
+
+/* Runs nsteps steps back to back (the graph's kernels, launched one by one)
+ * with CUDA events between phases on the context's stream; returns the total
+ * device time and the per-phase sums in milliseconds: [0] keys, sort, reorder,
+ * cell ranges, IDIC-key sort; [1] density, EOS, t_stop, step size; [2] force
+ * sweep; [3] IDIC reduce + solve, relax, move, energy. */
+ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms);
+
+/* Number of kernels one step launches (the library's own kernels). */
+ds_status ds_kernels_per_step(ds_ctx *c, int *count);
+
+/* Device bytes held by the context, and particles per tube. */
+ds_status ds_memory_bytes(ds_ctx *c, long long *bytes);
+
+/* Sticky device flags (DS_FLAG_*) and the last error text. */
+ds_status ds_last_error(ds_ctx *c, int *device_flags, char *msg, int msglen);
+
+/* Pinned host memory for end-to-end copies (cudaMallocHost / cudaFreeHost). */
+ds_status ds_host_alloc(void **ptr, long long bytes);
+ds_status ds_host_free(void *ptr);
+
+void ds_destroy(ds_ctx *c);
+
+/* Library version string. */
+const char *ds_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

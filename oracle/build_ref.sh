@@ -18,10 +18,10 @@ if [ ! -f "$REF/kernel.cu" ] || [ ! -f "$REF/IDIC.h" ] || [ ! -f "$REF/data.h" ]
   exit 3
 fi
 mkdir -p "$OUT"
+# the rewritten text is piped straight into the compiler (no copy is written)
 sed -E -e 's/([A-Za-z_][A-Za-z_0-9]*)[[:space:]]*<<[[:space:]]*<([^>]*)>>[[:space:]]*>/ds_ref_launch(\2, \1)/g' \
   -e 's/\\Nn /Nn /g' \
-  "$REF/kernel.cu" > "$OUT/kernel_host.cpp"
-g++ -O2 -fopenmp -ffp-contract=off -w -std=c++17 \
-  -I "$HERE/ref_include" -I "$REF" \
-  "$OUT/kernel_host.cpp" -o "$OUT/dustyshock_ref" -lm
+  "$REF/kernel.cu" |
+  g++ -O2 -fopenmp -ffp-contract=off -w -std=c++17 \
+    -I "$HERE/ref_include" -I "$REF" -x c++ - -o "$OUT/dustyshock_ref" -lm
 echo "$OUT/dustyshock_ref"

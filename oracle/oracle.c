@@ -365,6 +365,7 @@ void orc_idic_solve_cell(int n, const double *eps, const double *t, double vg, c
 int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken) {
   orc_grid G;
   orc_grid_setup(P, &G);
+  if ((G.per_y && G.ny < 3) || (G.per_z && G.nz < 3)) return -1; /* periodic axis needs >= 3 cells */
   const int nd = P->n_dust, ns = 1 + nd;
   orc_species *gas = &sp[0];
   const int Ng = gas->n;
@@ -388,11 +389,12 @@ int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken)
    * dust's own Ind. */
   for (int i = 0; i < Ng; i++)
     if (gas->ind[i] == 0) gas->rho[i] = 0.0;
-  for (int s = 1; s < ns; s++)
-    for (int i = 0; i < sp[s].n; i++) {
-      int z = coupled ? (i < Ng && gas->ind[i] == 0) : (sp[s].ind[i] == 0);
-      if (z) sp[s].rho[i] = 0.0;
-    }
+  if (P->flags & ORC_DUST_RHO) /* dust rho is output only; untouched when not computed */
+    for (int s = 1; s < ns; s++)
+      for (int i = 0; i < sp[s].n; i++) {
+        int z = coupled ? (i < Ng && gas->ind[i] == 0) : (sp[s].ind[i] == 0);
+        if (z) sp[s].rho[i] = 0.0;
+      }
 
   /* gas density + EOS (kernel.cu:2011-2024) */
   {

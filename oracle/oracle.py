@@ -184,7 +184,10 @@ class OracleState:
         Tm = ctypes.c_double(self.Tm)
         dt = ctypes.c_double(0.0)
         for _ in range(n):
-            self.last_status |= L.orc_step(ctypes.byref(self.P), self._arr, ctypes.byref(Tm), ctypes.byref(dt))
+            st = L.orc_step(ctypes.byref(self.P), self._arr, ctypes.byref(Tm), ctypes.byref(dt))
+            if st < 0:
+                raise ValueError("oracle: a periodic axis has fewer than 3 neighbour cells")
+            self.last_status |= st
         self.Tm = Tm.value
         self.last_dt = dt.value
         return self

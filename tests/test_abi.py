@@ -1,0 +1,66 @@
+"""The C-ABI library builds, loads and exports every symbol of include/*.h (no GPU needed)."""
+import ctypes
+import os
+import re
+
+from dustyshock3d_gb300 import _lib
+from dustyshock3d_gb300 import build as dsbuild
+from dustyshock3d_gb300.params import MODE_BITS
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "dustyshock3d_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ds_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    dsbuild.build()
+    L = ctypes.CDLL(dsbuild.LIB)
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
+
+
+def test_params_struct_layout_matches_header():
+    # sizeof(ds_params): 6+1 doubles... computed by the compiler in a tiny TU
+    import subprocess, tempfile
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        open(src, "w").write('#include "dustyshock3d_gb300.h"\n#include <stdio.h>\n#include <stddef.h>\n'
+                             'int main(){printf("%zu %zu %zu %zu\\n", sizeof(ds_params), offsetof(ds_params, n_dust),'
+                             ' offsetof(ds_params, cell_w), offsetof(ds_params, eps_empty));return 0;}\n')
+        exe = os.path.join(d, "t")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    c = _lib.DsParams
+    assert [int(x) for x in out] == [ctypes.sizeof(c), c.n_dust.offset, c.cell_w.offset, c.eps_empty.offset]
+
+
+def test_mode_bits_match_header():
+    text = open(HEADER).read()
+    hdr = {m.group(1).lower(): int(m.group(2), 16) for m in re.finditer(r"#define DS_MODE_([A-Z_0-9]+) (0x[0-9a-f]+)", text)}
+    for name, bit in MODE_BITS.items():
+        assert hdr[name] == bit, name
+
+
+def test_params_init_and_init_txt_reader(tmp_path):
+    L = _lib.load()
+    p = _lib.DsParams()
+    assert L.ds_params_init(ctypes.byref(p)) == 0
+    assert p.Gam_g == 1.4 and p.n_dust == 2 and p.mass_ratio[1] == 0.5
+    f = tmp_path / "Init.txt"
+    f.write_text("// Initial parameters\n-1.5\t// X_min\n1.5\n-0.5\n0.5\n-0.25\n0.75\n1\t// eos\n5000\n20\n0.07\n0.5\n"
+                 "2.5e-3\n0.3\n0.05\n0.5\n1.5\n0.02\n")
+    assert L.ds_params_read_init_txt(str(f).encode(), ctypes.byref(p)) == 0
+    assert (p.X_min, p.Z_max, p.Type_of_state, p.Maximum_particle, p.h, p.tau, p.eps) == \
+        (-1.5, 0.75, 1, 5000, 0.07, 2.5e-3, 0.02)
+
+
+def test_version_string():
+    assert b"sm_103a" in _lib.load().ds_version()

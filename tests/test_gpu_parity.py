@@ -1,0 +1,198 @@
+"""CUDA path against the oracle and the reference's own snapshots (needs a GPU).
+
+Bit-exactness claims:
+  * cell keys, the reference's linked lists (head / next) and per-particle
+    candidate / in-range counts equal the oracle's exactly (integers);
+  * the FP64 path equals the oracle bit for bit after N steps (same operation
+    and summation order, no FMA contraction) -- floats compared with ==;
+  * the FP32 path is compared with a stated tolerance.
+"""
+import numpy as np
+import pytest
+
+from dustyshock3d_gb300 import ic
+from dustyshock3d_gb300.solver import Solver
+from oracle.oracle import OracleState
+from tests._golden import NAMES, assert_close_nan, setup, snapshot_steps
+
+pytestmark = pytest.mark.gpu
+
+GAS_F = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e")
+DUST_F = ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")
+
+
+def run_gpu(P, species, nsteps):
+    with Solver(P) as S:
+        S.set_tube(0, species)
+        if nsteps:
+            S.step(nsteps)
+        out = [S.get_species(0, s) for s in range(len(species))]
+        t = S.time(0)
+    return out, t
+
+
+def assert_equal_nan(a, b, what):
+    a = np.asarray(a); b = np.asarray(b)
+    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    if not same.all():
+        bad = np.nonzero(~same)[0]
+        err = np.nanmax(np.abs(a[bad] - b[bad])) if len(bad) else 0
+        raise AssertionError(f"{what}: {len(bad)} of {len(a)} differ (max |diff| {err:.3e}), first {bad[:5]}")
+
+
+def compare_exact(gpu, orc, tag):
+    for f in GAS_F:
+        assert_equal_nan(getattr(gpu[0], f), getattr(orc[0], f), f"{tag} gas {f}")
+    for k in range(1, len(orc)):
+        for f in DUST_F:
+            assert_equal_nan(getattr(gpu[k], f), getattr(orc[k], f), f"{tag} dust{k} {f}")
+    assert (gpu[0].ind == orc[0].ind).all()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_lists_and_counts_bitexact(name):
+    g, P, sp = setup(name)
+    O = OracleState(P, sp)
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        for s in range(3):
+            dbg = S.debug_cells(0, s)
+            head, nxt = O.lists(s)
+            assert (dbg["cell_key"] == O.cell_keys(s)).all(), f"species {s} cell keys"
+            assert dbg["ncells"] + 1 == len(head)
+            assert (dbg["head"] == head).all(), f"species {s} list heads"
+            assert (dbg["next"] == nxt).all(), f"species {s} next pointers"
+            nc, nn = O.neighbour_counts(s)
+            assert (dbg["ncand"] == nc).all(), f"species {s} candidate counts"
+            assert (dbg["nnb"] == nn).all(), f"species {s} in-range counts"
+        # lists again after two steps (particles have moved)
+        S.step(2)
+        O.step(2)
+        for s in range(3):
+            dbg = S.debug_cells(0, s)
+            head, nxt = O.lists(s)
+            assert (dbg["head"] == head).all() and (dbg["next"] == nxt).all()
+
+
+@pytest.mark.parametrize("name,nsteps", [("refA", 3), ("refB", 10), ("refC", 10)])
+def test_reference_mode_fp64_bitexact(name, nsteps):
+    g, P, sp = setup(name)
+    gpu, (Tm, dt, ns) = run_gpu(P, sp, nsteps)
+    O = OracleState(P, sp).step(nsteps)
+    assert ns == nsteps
+    assert Tm == O.Tm
+    compare_exact(gpu, O.species, name)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_replays_reference_snapshots(name):
+    """The CUDA path against what the reference program itself printed."""
+    g, P, sp = setup(name)
+    nsnap = len(g["snap_times"])
+    steps = snapshot_steps(P, nsnap)
+    interior = g["ind"] == 0
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        done = 0
+        for s, target in enumerate(steps, start=1):
+            S.step(target - done)
+            done = target
+            gas = S.get_species(0, 0)
+            for col, arr in (("x", gas.x), ("rho", gas.rho), ("p", gas.p), ("Vx", gas.vx), ("Vy", gas.vy),
+                             ("e", gas.e)):
+                assert_close_nan(arr[interior], g[f"s{s}_gas_{col}"], 1e-8, f"{name} s{s} gas {col}")
+            for k in (1, 2):
+                d = S.get_species(0, k)
+                for col, arr in (("x", d.x), ("rho", d.rho), ("t_stop", d.ts), ("Vx", d.vx)):
+                    assert_close_nan(arr[interior], g[f"s{s}_d{k}_{col}"], 1e-8, f"{name} s{s} dust{k} {col}")
+
+
+def small_tube(**kw):
+    args = dict(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25))
+    args.update(kw)
+    return ic.dusty_sod_tube(**args)
+
+
+@pytest.mark.parametrize("eps,t_s", [(1.0, 1e-3), (0.01, 1e-1), (10.0, 1e-4)])
+def test_baseline_mode_fp64_bitexact(eps, t_s):
+    P, sp = small_tube(eps=eps, t_s=t_s)
+    gpu, (Tm, dt, ns) = run_gpu(P, sp, 6)
+    O = OracleState(P, sp).step(6)
+    assert Tm == O.Tm and dt == O.last_dt
+    compare_exact(gpu, O.species, f"eps={eps} ts={t_s}")
+
+
+def test_baseline_lists_and_counts_bitexact():
+    P, sp = small_tube()
+    O = OracleState(P, sp).step(3)
+    with Solver(P) as S:
+        S.set_tube(0, O.species)
+        for s in range(2):
+            dbg = S.debug_cells(0, s)
+            head, nxt = O.lists(s)
+            assert (dbg["cell_key"] == O.cell_keys(s)).all()
+            assert (dbg["head"] == head).all() and (dbg["next"] == nxt).all()
+            nc, nn = O.neighbour_counts(s)
+            assert (dbg["ncand"] == nc).all() and (dbg["nnb"] == nn).all()
+
+
+def test_fp32_path_against_fp64_oracle():
+    """FP32 sweeps (Kahan sums, cell-relative FP32 positions) vs the FP64 oracle:
+    relative L1 of gas density <= 1e-5 after 10 steps, velocities <= 1e-4 of the
+    velocity scale."""
+    P, sp = small_tube()
+    P32 = P.copy()
+    P32.precision = "fp32"
+    gpu, _ = run_gpu(P32, sp, 10)
+    O = OracleState(P, sp).step(10)
+    g, o = gpu[0], O.species[0]
+    l1 = np.abs(g.rho - o.rho).sum() / np.abs(o.rho).sum()
+    assert l1 < 1e-5, l1
+    vscale = np.abs(o.vx).max()
+    assert np.abs(g.vx - o.vx).mean() / vscale < 1e-4
+    assert np.abs(gpu[1].vx - O.species[1].vx).mean() / vscale < 1e-4
+
+
+def test_batched_tubes_equal_single_runs():
+    cases = [small_tube(eps=1.0, t_s=1e-3), small_tube(eps=0.1, t_s=1e-2, rho_R=0.25, p_R=0.2),
+             small_tube(dx_left=1 / 48, Ly=0.375, eps=3.0, t_s=3e-4)]
+    with Solver([c[0] for c in cases]) as S:
+        for t, (P, sp) in enumerate(cases):
+            S.set_tube(t, sp)
+        S.step(5)
+        batched = [[S.get_species(t, s) for s in range(2)] for t in range(len(cases))]
+    for t, (P, sp) in enumerate(cases):
+        alone, _ = run_gpu(P, sp, 5)
+        compare_exact(batched[t], alone, f"tube {t}")
+
+
+def test_time_loop_stops_at_t_end():
+    P, sp = small_tube()
+    P.T_end = 0.02
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(100)
+        Tm, dt, ns = S.time(0)
+    assert Tm == pytest.approx(0.02, rel=0, abs=1e-15) and ns < 100
+
+
+def test_upload_download_roundtrip_preserves_order():
+    P, sp = small_tube()
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(1)
+        a = S.get_species(0, 0)
+        # upload the downloaded state again; one more step must equal two steps straight
+        S2 = Solver(P)
+        S2.set_tube(0, sp)
+        S2.step(2)
+        b = S2.get_species(0, 0)
+        S2.close()
+        a.m, a.h = sp[0].m, sp[0].h
+        d = S.get_species(0, 1)
+        d.m, d.h = sp[1].m, sp[1].h
+        S.set_tube(0, [a, d])
+        S.step(1)
+        c = S.get_species(0, 0)
+    for f in ("x", "vx", "rho", "e"):
+        assert_equal_nan(getattr(c, f), getattr(b, f), f)
