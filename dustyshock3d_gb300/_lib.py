@@ -69,6 +69,8 @@ SIGNATURES = {
     "ds_kernels_per_step": ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "ds_memory_bytes": ([_VP, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "ds_last_error": ([_VP, _IP, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+    "ds_cell_lists_noalloc": ([ctypes.POINTER(DsParams), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
+                               _VP, _VP], ctypes.c_int),
     "ds_host_alloc": ([ctypes.POINTER(_VP), ctypes.c_longlong], ctypes.c_int),
     "ds_host_free": ([_VP], ctypes.c_int),
     "ds_destroy": ([_VP], None),

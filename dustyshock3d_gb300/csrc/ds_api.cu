@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -856,3 +857,111 @@ void ds_destroy(ds_ctx *c) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free cell lists (ds_cell_lists_noalloc)
+//
+// For callers that cannot call cudaMalloc: a host whose device memory is all
+// handed to its own pool allocator, or code that runs where an allocation
+// would be an error or would stall the device (cudaMalloc can synchronise the
+// whole device).  The sort's scratch (keys, values, their alternates and the
+// radix histograms) lives in the file-scope array below instead of in
+// context-owned memory.  It is sized for DS_NOALLOC_MAX_PARTICLES particles
+// (about 4.3 MB), and every GPU that loads this library holds it until the
+// process exits.  All calls share it: calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on it.  Every scratch
+// word a call reads has been written earlier in the same call, so nothing
+// needs clearing between calls.
+// ===========================================================================
+namespace {
+
+constexpr int kNaTile = 2048;  // keys per radix tile (ds_sort.cu)
+constexpr int kNaMax = DS_NOALLOC_MAX_PARTICLES;
+constexpr size_t kNaHistWords = 256 * (size_t)((kNaMax + kNaTile - 1) / kNaTile) + 256;
+constexpr size_t kNaWords = 4 * (size_t)kNaMax + kNaHistWords;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
+
+std::mutex g_noalloc_mu;
+uint32_t *g_noalloc_ptr[256] = {};
+
+// The device address of the scratch array for the current device.  The host
+// symbol is only a stand-in: it is resolved with cudaGetSymbolAddress once per
+// device (on the first call made with that device current).
+ds_status noalloc_scratch(uint32_t **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return DS_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return DS_ERR_CUDA;
+    g_noalloc_ptr[dev] = (uint32_t *)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return DS_OK;
+}
+
+__global__ void k_na_keys(const TubeDesc T, const double *x, const double *y, const double *z, int n,
+                          int *cell_key, uint32_t *kin, uint32_t *vin) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int raw = ds_raw_key(T, x[i], y[i], z[i]);
+  cell_key[i] = raw;
+  int local;
+  if (!(T.mode & M_GRID_PROPER))
+    local = (raw >= 0 && raw <= T.ncells) ? raw : T.ncells + 1;  // kernel.cu:1950
+  else
+    local = raw >= 0 ? raw : T.ncells + 1;
+  kin[i] = (uint32_t)local;
+  vin[i] = (uint32_t)i;
+}
+
+__global__ void k_na_fill(int *a, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+// head[c] = first particle of cell c, next[p] = following particle of p's cell
+// in ascending index, -1 at the end and for unlisted particles.
+__global__ void k_na_lists(const uint32_t *skey, const uint32_t *sidx, int n, int ncells, int *head, int *next) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint32_t k = skey[q];
+  const int p = (int)sidx[q];
+  if ((int)k > ncells) {
+    next[p] = -1;
+    return;
+  }
+  if (q == 0 || skey[q - 1] != k) head[k] = p;
+  next[p] = (q + 1 < n && skey[q + 1] == k) ? (int)sidx[q + 1] : -1;
+}
+
+}  // namespace
+
+extern "C" ds_status ds_cell_lists_noalloc(const ds_params *p, int n, const double *d_x, const double *d_y,
+                                           const double *d_z, int *d_cell_key, int *d_head, int head_len,
+                                           int *d_next, void *stream) {
+  if (!p || n < 0 || !d_head) return DS_ERR_ARG;
+  if (n > kNaMax) return DS_ERR_ARG;  // beyond the static scratch
+  if (n > 0 && (!d_x || !d_y || !d_z || !d_cell_key || !d_next)) return DS_ERR_ARG;
+  if (check_params(nullptr, *p) != DS_OK) return DS_ERR_ARG;
+  TubeDesc T;
+  build_desc(*p, T);
+  if (head_len < T.ncells + 1) return DS_ERR_ARG;
+  if (ds_radix_scratch_words(n > 0 ? n : 1) > kNaHistWords) return DS_ERR_ARG;
+  uint32_t *s = nullptr;
+  ds_status st = noalloc_scratch(&s);
+  if (st != DS_OK) return st;
+  uint32_t *kin = s, *vin = s + kNaMax, *kalt = s + 2 * (size_t)kNaMax, *valt = s + 3 * (size_t)kNaMax;
+  uint32_t *hist = s + 4 * (size_t)kNaMax;
+  cudaStream_t cs = (cudaStream_t)stream;
+  const int nh = T.ncells + 1;
+  k_na_fill<<<(nh + 255) / 256, 256, 0, cs>>>(d_head, nh, -1);
+  if (n > 0) {
+    k_na_keys<<<(n + 255) / 256, 256, 0, cs>>>(T, d_x, d_y, d_z, n, d_cell_key, kin, vin);
+    bool alt = false;
+    ds_radix_sort(kin, vin, kalt, valt, n, bits_for((long long)T.ncells + 2), hist, cs, &alt);
+    k_na_lists<<<(n + 255) / 256, 256, 0, cs>>>(alt ? kalt : kin, alt ? valt : vin, n, T.ncells, d_head, d_next);
+  }
+  return cudaGetLastError() == cudaSuccess ? DS_OK : DS_ERR_CUDA;
+}

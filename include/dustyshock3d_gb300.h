@@ -193,6 +193,32 @@ ds_status ds_memory_bytes(ds_ctx *c, long long *bytes);
 /* Sticky device flags (DS_FLAG_*) and the last error text. */
 ds_status ds_last_error(ds_ctx *c, int *device_flags, char *msg, int msglen);
 
+/* Allocation-free cell lists.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc (a host that hands all device
+ * memory to its own pool allocator, or code that runs where an allocation
+ * would be an error or would stall the device): builds, for n particles whose
+ * positions are already in device memory, the raw cell key of each particle
+ * (kernel.cu:1949) and the reference's linked lists -- head[c] = first
+ * particle of cell c, next[p] = the following particle of p's cell in
+ * ascending index, -1 at the end (kernel.cu:1937-1955) -- exactly as
+ * ds_debug_cells reports them, without allocating anything.  The sort's
+ * scratch is a static device array inside the library sized for
+ * DS_NOALLOC_MAX_PARTICLES particles (about 4.3 MB per GPU that loads the
+ * library, held until the process exits); larger n returns DS_ERR_ARG.
+ * Inputs and outputs are caller-owned device arrays: d_cell_key[n],
+ * d_next[n], d_head[head_len] with head_len >= Number_of_fihd_cells + 1.
+ * The grid comes from p (cell width, box, DS_MODE_GRID_PROPER/PERIODIC_*).
+ * Work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and the call returns without waiting.  The first call on each device
+ * resolves the scratch array's device address; make that first call before
+ * any stream capture.  All calls share the one scratch array, so calls whose
+ * work overlaps on the GPU race; serialise them. */
+#define DS_NOALLOC_MAX_PARTICLES 262144
+ds_status ds_cell_lists_noalloc(const ds_params *p, int n, const double *d_x, const double *d_y,
+                                const double *d_z, int *d_cell_key, int *d_head, int head_len, int *d_next,
+                                void *stream);
+
 /* Pinned host memory for end-to-end copies (cudaMallocHost / cudaFreeHost). */
 ds_status ds_host_alloc(void **ptr, long long bytes);
 ds_status ds_host_free(void *ptr);
