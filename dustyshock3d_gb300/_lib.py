@@ -31,7 +31,7 @@ class DsParams(ctypes.Structure):
         ("tau", ctypes.c_double), ("T_end", ctypes.c_double), ("T_out", ctypes.c_double),
         ("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("eps", ctypes.c_double),
         ("Gam_g", ctypes.c_double), ("Speed_of_sound_gas", ctypes.c_double),
-        ("n_dust", ctypes.c_int), ("mode", ctypes.c_int), ("precision", ctypes.c_int), ("reserved0", ctypes.c_int),
+        ("n_dust", ctypes.c_int), ("mode", ctypes.c_int), ("precision", ctypes.c_int), ("stencil", ctypes.c_int),
         ("cell_w", ctypes.c_double), ("idic_w", ctypes.c_double), ("cfl", ctypes.c_double),
         ("t_empty", ctypes.c_double),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
@@ -117,6 +117,7 @@ def params_to_c(P: Params) -> DsParams:
             mode |= bit
     c.mode = mode
     c.precision = 1 if str(P.precision).lower() in ("fp32", "1") else 0
+    c.stencil = int(getattr(P, "stencil", 1) or 1)
     for k in range(MAX_DUST):
         c.mass_ratio[k] = float(P.mass_ratio[k]) if k < len(P.mass_ratio) else 0.0
         c.R_dust[k] = float(P.R_dust[k]) if k < len(P.R_dust) else 0.0

@@ -57,7 +57,7 @@ struct ds_ctx {
   std::string msg;
   // sizes
   int N = 0;
-  int nkeys = 0, key_bits = 0, nikeys = 0, ikey_bits = 0, ncell_total = 0, nseg = 0;
+  int nkeys = 0, key_bits = 0, nikeys = 0, ikey_bits = 0, ncell_total = 0, nseg = 0, nnseg = 0;
   std::vector<TubeDesc> tdesc;
   std::vector<Chunk> ch_all, ch_gas, ch_dust;
   // device
@@ -69,6 +69,11 @@ struct ds_ctx {
   TubeState *d_tstate = nullptr;
   Chunk *d_ch_all = nullptr, *d_ch_gas = nullptr, *d_ch_dust = nullptr;
   int *d_seg_key0 = nullptr, *d_seg_species = nullptr, *d_seg_orphan = nullptr, *d_tube_cell0 = nullptr;
+  int *d_nseg_key0 = nullptr, *d_nseg_tube = nullptr, *d_nseg_species = nullptr;
+  double *hmax = nullptr;
+  unsigned char *krad = nullptr;
+  const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
+  bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
   double *cs64 = nullptr, *pt64 = nullptr, *edot = nullptr;
   uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
@@ -188,6 +193,10 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   // FP32 screen slack: rounding of |coordinate| <= L (or <= 2 cell widths when
   // cell-relative) in each of the two operands, with a 5x margin
   T.pre_abs = (float)(1e-6 * (proper ? 4.0 * wmax : L));
+  T.stencil = (P.stencil == 2 && proper) ? 2 : 1;
+  const double wmin = fmin(T.wx, fmin(T.wy, T.wz));
+  T.r1_hmax = T.stencil == 2 ? 0.5 * wmin * (1.0 - 1e-9) : 1e300;
+  T.inv_wx = 1.0 / T.wx; T.inv_wy = 1.0 / T.wy; T.inv_wz = 1.0 / T.wz; T.inv_aw = 1.0 / T.aw;
 }
 
 ds_status check_params(ds_ctx *c, const ds_params &P) {
@@ -205,8 +214,12 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
   if (T.Cnx < 0 || T.Cny < 0 || T.Cnz < 0) return fail(c, DS_ERR_ARG, "box extent must be positive");
   if (T.ncells <= 0 || T.ncells > (1 << 28)) return fail(c, DS_ERR_ARG, "neighbour grid too large");
   if (T.n_idic <= 0 || T.n_idic > (1 << 28)) return fail(c, DS_ERR_ARG, "IDIC grid too large");
-  if ((P.mode & DS_MODE_PERIODIC_Y) && T.ny < 3) return fail(c, DS_ERR_ARG, "periodic y needs >= 3 cells");
-  if ((P.mode & DS_MODE_PERIODIC_Z) && T.nz < 3) return fail(c, DS_ERR_ARG, "periodic z needs >= 3 cells");
+  if (P.stencil != 0 && P.stencil != 1 && P.stencil != 2) return fail(c, DS_ERR_ARG, "stencil must be 1 or 2");
+  if (P.stencil == 2 && !(P.mode & DS_MODE_GRID_PROPER))
+    return fail(c, DS_ERR_UNSUPPORTED, "stencil 2 needs the proper cell grid (DS_MODE_GRID_PROPER)");
+  const int need = 2 * T.stencil + 1;  // a periodic axis must not alias its own stencil
+  if ((P.mode & DS_MODE_PERIODIC_Y) && T.ny < need) return fail(c, DS_ERR_ARG, "too few cells across periodic y");
+  if ((P.mode & DS_MODE_PERIODIC_Z) && T.nz < need) return fail(c, DS_ERR_ARG, "too few cells across periodic z");
   return DS_OK;
 }
 
@@ -236,6 +249,8 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.edot = c->edot;
   a.ncand = c->ncand;
   a.nnb = c->nnb;
+  a.skey = c->skey;
+  a.krad = c->krad;
   a.gas_slot_of_pid = c->slot_of_pid;
   a.gas_ind_pid = c->ind_of_pid;
   a.tstate_rw = c->d_tstate;
@@ -243,19 +258,26 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   return a;
 }
 
-// Sort + reorder + cell ranges for the particles' current positions; flips parity.
-void enqueue_sort(ds_ctx *c) {
+// Sort + reorder + cell ranges for the particles' current positions; flips
+// parity.  exact_order: cells list their particles in caller-index order even
+// on the FP32 path (the parity hook's lists).
+void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   cudaStream_t s = c->stream;
   DevState src = c->buf[c->parity].view();
   DevState dst = c->buf[c->parity ^ 1].view();
-  ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, s);
+  const bool fast = c->any_fp32 && !exact_order;
+  ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s);
   bool alt = false;
   ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits, c->rs_scratch, s, &alt);
   const uint32_t *skey = alt ? c->kalt : c->kin;
   const uint32_t *sval = alt ? c->valt : c->vin;
-  ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, src, dst, c->pos32, c->vm32,
-                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, s);
+  ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
+                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, fast, s);
   ds_launch_cell_start(skey, c->N, c->nkeys, c->cell_start, s);
+  c->skey = skey;
+  if (c->any_stencil2)
+    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->hmax, c->d_nseg_key0, c->d_nseg_tube,
+                          c->d_nseg_species, c->nnseg, c->krad, s);
   c->parity ^= 1;
 }
 
@@ -265,7 +287,6 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
   bool alt = false;
   ds_radix_sort(c->ikin, c->ivin, c->ikalt, c->ivalt, c->N, c->ikey_bits, c->rs_scratch, s, &alt);
   c->isort_alt = alt;
-  cudaMemsetAsync(c->ca.cnt, 0, sizeof(int) * (size_t)c->nikeys, s);
   if (ev) cudaEventRecord(ev[1], s);
   const bool fp32 = c->any_fp32;
   SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
@@ -285,10 +306,11 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[3], s);
   const uint32_t *ik = alt ? c->ikalt : c->ikin;
   const uint32_t *iv = alt ? c->ivalt : c->ivin;
-  ds_launch_idic_reduce(ik, iv, c->N, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st, c->ca, s);
-  ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, s);
+  ds_launch_idic_reduce(ik, iv, c->N, c->nikeys, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st,
+                        c->ca, s);
+  ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, fp32, s);
   ds_launch_relax_move(c->d_tubes, c->d_tstate, c->d_ch_all, (int)c->ch_all.size(), st, c->idic_local, c->edot,
-                       c->ca, c->d_flags, s);
+                       c->ca, c->d_flags, fp32, s);
   ds_launch_step_end(c->d_tstate, c->ntubes, s);
 }
 
@@ -305,7 +327,7 @@ ds_status finalize(ds_ctx *c) {
   CK(cudaSetDevice(c->device));
   // segments, keys
   c->tdesc.assign(c->ntubes, TubeDesc{});
-  std::vector<int> seg_key0, seg_species, seg_orphan, tube_cell0;
+  std::vector<int> seg_key0, seg_species, seg_orphan, tube_cell0, nseg_key0, nseg_tube, nseg_species;
   int N = 0;
   long long nkeys = 0, nikeys = 0, ncell = 0;
   for (int t = 0; t < c->ntubes; t++) {
@@ -321,6 +343,9 @@ ds_status finalize(ds_ctx *c) {
       N += H.n;
       T.seg_end[s] = N;
       T.key_base[s] = (int)nkeys;
+      nseg_key0.push_back((int)nkeys);
+      nseg_tube.push_back(t);
+      nseg_species.push_back(s);
       nkeys += T.ncells + 2;
       T.idic_base[s] = (int)nikeys;
       seg_key0.push_back((int)nikeys);
@@ -336,8 +361,10 @@ ds_status finalize(ds_ctx *c) {
     if (P.mode & DS_MODE_GRID_PROPER) c->any_proper = true;
     if (P.mode & DS_MODE_DUST_RHO) c->any_dust_rho = true;
     if (P.precision == DS_PRECISION_FP32) c->any_fp32 = true;
+    if (T.stencil == 2) c->any_stencil2 = true;
   }
   if (nkeys >= (1LL << 31) || nikeys >= (1LL << 31)) return fail(c, DS_ERR_ARG, "key space too large");
+  if (N >= (1 << 25)) return fail(c, DS_ERR_UNSUPPORTED, "more than 2^25 particles in one context");
   // one kernel variant per batch: the mode bits that select templates must agree
   for (int t = 1; t < c->ntubes; t++) {
     const ds_params &P = c->params[t];
@@ -366,12 +393,16 @@ ds_status finalize(ds_ctx *c) {
   DA(c->slot_of_pid, N); DA(c->ind_of_pid, N); DA(c->idic_local, N);
   DA(c->cell_start, (size_t)nkeys + 1);
   DA(c->ncand, N); DA(c->nnb, N);
+  DA(c->hmax, (size_t)nkeys);
+  DA(c->krad, (size_t)nkeys);
+  CK(cudaMemsetAsync(c->krad, 1, (size_t)nkeys, c->stream));
   DA(c->stage, N);
   DA(c->d_cons, 8);
   DA(c->d_flags, 1);
   DA(c->ca.cnt, nikeys);
-  double **cd[] = {&c->ca.vx, &c->ca.vy, &c->ca.vz, &c->ca.a0, &c->ca.a1, &c->ca.a2,
-                   &c->ca.nvx, &c->ca.nvy, &c->ca.nvz, &c->ca.px, &c->ca.py, &c->ca.pz};
+  DA(c->ca.start, (size_t)nikeys + 1);
+  double **cd[] = {&c->ca.vx, &c->ca.vy, &c->ca.vz, &c->ca.a0, &c->ca.a1, &c->ca.a2, &c->ca.nvx, &c->ca.nvy,
+                   &c->ca.nvz, &c->ca.px, &c->ca.py, &c->ca.pz, &c->ca.q0, &c->ca.q1};
   for (double **p : cd) DA(*p, nikeys);
   CK(cudaMemsetAsync(c->ca.cnt, 0, sizeof(int) * (size_t)nikeys, c->stream));
   for (double **p : cd) CK(cudaMemsetAsync(*p, 0, sizeof(double) * (size_t)nikeys, c->stream));
@@ -390,6 +421,10 @@ ds_status finalize(ds_ctx *c) {
   if ((st = upload_vec(c, &c->d_seg_species, seg_species)) != DS_OK) return st;
   if ((st = upload_vec(c, &c->d_seg_orphan, seg_orphan)) != DS_OK) return st;
   if ((st = upload_vec(c, &c->d_tube_cell0, tube_cell0)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_nseg_key0, nseg_key0)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_nseg_tube, nseg_tube)) != DS_OK) return st;
+  if ((st = upload_vec(c, &c->d_nseg_species, nseg_species)) != DS_OK) return st;
+  c->nnseg = (int)nseg_key0.size();
   // particles: slot = segment begin + caller index
   c->parity = 0;
   for (int t = 0; t < c->ntubes; t++)
@@ -693,7 +728,8 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   if (st != DS_OK) return st;
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
-  *count = 12 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0);
+  *count = 13 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
+           (c->any_stencil2 ? 2 : 0);
   return DS_OK;
 }
 
@@ -747,7 +783,7 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
   const TubeDesc &T = c->tdesc[tube];
   const int b = T.seg_begin[species], n = T.seg_end[species] - b;
   if (ncells) *ncells = T.ncells;
-  enqueue_sort(c);  // lists for the current positions
+  enqueue_sort(c, true);  // lists for the current positions, caller-index order
   if (ncand || nnb) {
     std::vector<Chunk> ch;
     add_chunks(ch, tube, species, b, b + n);

@@ -38,9 +38,34 @@ __global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
   ts[t].dt = 0.0;
 }
 
+// Per-axis cell of a position in the proper grid, FP32 path: reciprocal
+// multiplies instead of FP64 divisions (GB300's FP64 divide is ~20x an FP32
+// multiply-add); periodic axes clamped.  Every cell index of the FP32 path
+// comes from here or from the sorted keys, so they are consistent.
+__device__ __forceinline__ void fast_proper_cell(const TubeDesc &T, double x, double y, double z, int &ix, int &iy,
+                                                 int &iz) {
+  ix = (int)floor((x - T.ox) * T.inv_wx);
+  iy = (int)floor((y - T.oy) * T.inv_wy);
+  iz = (int)floor((z - T.oz) * T.inv_wz);
+  if (T.mode & M_PER_Y) { iy = iy < 0 ? 0 : iy; iy = iy >= T.ny ? T.ny - 1 : iy; }
+  if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
+}
+
+__device__ __forceinline__ int fast_idic_cell(const TubeDesc &T, double x, double y, double z) {
+  const int ix = (int)floor((x - T.ox) * T.inv_aw);
+  const int iy = (int)floor((y - T.oy) * T.inv_aw);
+  const int iz = (int)floor((z - T.oz) * T.inv_aw);
+  if (ix < 0 || ix >= T.anx || iy < 0 || iy >= T.any_ || iz < 0 || iz >= T.anz) return -1;
+  const int c = ix + iy * T.asy + iz * T.asz;
+  return (c < 0 || c > T.n_idic) ? -1 : c;
+}
+
 // Neighbour key of each slot (kernel.cu:1949; out-of-range keys are not
-// listed, kernel.cu:1950, and go to the orphan bucket ncells+1), written at
-// the particle's caller index so the stable sort keeps ascending index.
+// listed, kernel.cu:1950, and go to the orphan bucket ncells+1).  Reference
+// order: written at the particle's caller index, so the stable sort keeps
+// ascending index within a cell as the reference's lists do.  FP32 path:
+// written in slot order (coalesced); a cell then keeps its previous order.
+template <bool FAST>
 __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
                        uint32_t *vin) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -48,23 +73,33 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
     const int i = ch.begin + threadIdx.x;
     if (i >= ch.end) continue;
     const TubeDesc &T = tubes[ch.tube];
-    int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
     int local;
-    if (!(T.mode & M_GRID_PROPER))
-      local = (key >= 0 && key <= T.ncells) ? key : T.ncells + 1;
-    else
-      local = key >= 0 ? key : T.ncells + 1;
-    const int dst = T.seg_begin[ch.species] + st.pid[i];
+    if (FAST && (T.mode & M_GRID_PROPER)) {
+      int ix, iy, iz;
+      fast_proper_cell(T, st.x[i], st.y[i], st.z[i], ix, iy, iz);
+      const bool in = ix >= 0 && ix < T.nx && iy >= 0 && iy < T.ny && iz >= 0 && iz < T.nz;
+      local = in ? ix + iy * T.sy + iz * T.sz : T.ncells + 1;
+    } else {
+      const int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
+      if (!(T.mode & M_GRID_PROPER))
+        local = (key >= 0 && key <= T.ncells) ? key : T.ncells + 1;
+      else
+        local = key >= 0 ? key : T.ncells + 1;
+    }
+    const int dst = FAST ? i : T.seg_begin[ch.species] + st.pid[i];
     kin[dst] = (uint32_t)(T.key_base[ch.species] + local);
     vin[dst] = (uint32_t)i;
   }
 }
 
 // Gather every persistent field from the previous order (src) into the new
-// sorted order (dst); build the FP32 copies and the IDIC keys.
+// sorted order (dst); build the FP32 copies and the IDIC keys (reference
+// order: at the caller index, so the IDIC sums run in ascending index as the
+// reference's host loops do; FP32 path: in slot order).
+template <bool FAST>
 __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
-                          DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
-                          uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid) {
+                          const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32,
+                          int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int q = ch.begin + threadIdx.x;
@@ -83,14 +118,23 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     const int ind = src.ind[j], pid = src.pid[j];
     dst.ind[q] = ind; dst.pid[q] = pid;
     const int gp = T.seg_begin[ch.species] + pid;
-    slot_of_pid[gp] = q;
-    ind_of_pid[gp] = ind;
-    // FP32 coordinates: offsets from the own cell origin (proper grid) or from
-    // the tube's reference point (reference grid)
+    if (!(T.mode & M_TSTOP_CONST)) slot_of_pid[gp] = q;  // index-coupled stopping time (IDIC.h:86)
+    if (T.mode & M_REF_COUPLING) ind_of_pid[gp] = ind;    // index-coupled dust rho zeroing (IDIC.h:8)
+    // FP32 coordinates: offsets from the own (listed) cell's origin (proper
+    // grid), or from the tube's reference point (reference grid)
     float4 p4;
     if (T.cellrel) {
+      const int local = (int)skey[q] - T.key_base[ch.species];
       int ix, iy, iz;
-      ds_proper_cell(T, x, y, z, ix, iy, iz);
+      if (local < T.ncells) {
+        ix = local % T.nx;
+        iy = (local / T.nx) % T.ny;
+        iz = local / (T.nx * T.ny);
+      } else if (FAST) {
+        fast_proper_cell(T, x, y, z, ix, iy, iz);
+      } else {
+        ds_proper_cell(T, x, y, z, ix, iy, iz);
+      }
       p4.x = (float)(x - (T.ox + ix * T.wx));
       p4.y = (float)(y - (T.oy + iy * T.wy));
       p4.z = (float)(z - (T.oz + iz * T.wz));
@@ -102,10 +146,11 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     p4.w = (float)h;
     pos32[q] = p4;
     vm32[q] = make_float4((float)vx, (float)vy, (float)vz, (float)m);
-    const int ic = ds_idic_cell(T, x, y, z);
+    const int ic = FAST ? fast_idic_cell(T, x, y, z) : ds_idic_cell(T, x, y, z);
     idic_local[q] = ic;
-    ikin[gp] = (uint32_t)(T.idic_base[ch.species] + (ic >= 0 ? ic : T.n_idic + 1));
-    ivin[gp] = (uint32_t)q;
+    const int idst = FAST ? q : gp;
+    ikin[idst] = (uint32_t)(T.idic_base[ch.species] + (ic >= 0 ? ic : T.n_idic + 1));
+    ivin[idst] = (uint32_t)q;
   }
 }
 
@@ -128,36 +173,45 @@ __device__ __forceinline__ int find_seg(const int *seg_key0, int nseg, int key) 
   return lo;
 }
 
-// Per IDIC cell and species, sums in ascending particle index (the reference's
-// host loops, kernel.cu:2114-2123, 2137-2146, 2165-2174, 2294-2300).
-__global__ void k_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
-                              const int *seg_species, const int *seg_orphan, int nseg, DevState st,
-                              CellArrays ca) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const uint32_t key = ikey[q];
-  if (q > 0 && ikey[q - 1] == key) return;  // not the start of a run
-  const int sg = find_seg(seg_key0, nseg, (int)key);
-  if ((int)key == seg_orphan[sg]) return;    // outside the IDIC grid
+// Per IDIC cell and species (one thread per key; run bounds from start[]):
+// count and sums in the sorted order -- ascending particle index on the
+// reference path, as the reference's host loops sum (kernel.cu:2114-2123,
+// 2137-2146, 2165-2174, 2294-2300).  Empty cells get count 0.
+__global__ void k_idic_reduce(const uint32_t *islot, int nikeys, const int *seg_key0, const int *seg_species,
+                              const int *seg_orphan, int nseg, DevState st, CellArrays ca) {
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  if (key >= nikeys) return;
+  const int sg = find_seg(seg_key0, nseg, key);
+  if (key == seg_orphan[sg]) return;  // outside the IDIC grid
   const int s = seg_species[sg];
-  int cnt = 0;
+  const int r0 = ca.start[key], r1 = ca.start[key + 1];
   double vx = 0.0, vy = 0.0, vz = 0.0, a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for (int r = q; r < n && ikey[r] == key; r++) {
-    const int j = (int)islot[r];
-    cnt = cnt + 1;
-    if (s > 0) a0 = a0 + st.ts[j];
-    vx = vx + st.vx[j];
-    vy = vy + st.vy[j];
-    vz = vz + st.vz[j];
-    if (s == 0) {
+  if (s == 0) {
+#pragma unroll 4
+    for (int r = r0; r < r1; r++) {
+      const int j = (int)islot[r];
+      vx = vx + st.vx[j];
+      vy = vy + st.vy[j];
+      vz = vz + st.vz[j];
       a0 = a0 + st.ax[j];
       a1 = a1 + st.ay[j];
       a2 = a2 + st.az[j];
     }
+  } else {
+#pragma unroll 4
+    for (int r = r0; r < r1; r++) {
+      const int j = (int)islot[r];
+      a0 = a0 + st.ts[j];
+      vx = vx + st.vx[j];
+      vy = vy + st.vy[j];
+      vz = vz + st.vz[j];
+    }
   }
-  ca.cnt[key] = cnt;
-  ca.vx[key] = vx; ca.vy[key] = vy; ca.vz[key] = vz;
-  ca.a0[key] = a0; ca.a1[key] = a1; ca.a2[key] = a2;
+  ca.cnt[key] = r1 - r0;
+  if (r1 > r0) {
+    ca.vx[key] = vx; ca.vy[key] = vy; ca.vz[key] = vz;
+    ca.a0[key] = a0; ca.a1[key] = a1; ca.a2[key] = a2;
+  }
 }
 
 // One component of the per-cell implicit solve (kernel.cu:2310-2437); the
@@ -231,7 +285,7 @@ __device__ __forceinline__ void solve_comp(const double (&eps)[ND], const double
 // Per (tube, IDIC cell): means (kernel.cu:2126-2190), eps (2192-2211),
 // Psi (2302-2309), solve (2310-2437).  Results are written at the cell's key
 // of each species: new velocities; for gas Psi; for dust the mean t_stop and eps.
-template <int ND>
+template <int ND, bool FAST>
 __device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double tau, CellArrays &ca) {
   const int kg = T.idic_base[0] + c;
   const int cg = ca.cnt[kg];
@@ -270,8 +324,28 @@ __device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double
     ca.px[kd] = tt[k];   // dust: mean t_stop
     ca.py[kd] = eps[k];  // dust: eps
   }
+  if (FAST) {
+    // The relaxations of IDIC.h:276-313 rewritten as v_new = q0 v + q1 (...),
+    // coefficients per cell in FP64, so a particle needs no division:
+    //   dust  (v/tau + g/t)/(1/tau + 1/t) = t/(t+tau) v + tau/(t+tau) g
+    //   gas   (v/tau + N + a)/D, D = 1/tau + sum eps/t, N = sum eps v_k/t
+    double D = 1.0 / tau, Nx = 0.0, Ny = 0.0, Nz = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+      const int kd = T.idic_base[k + 1] + c;
+      const double w = eps[k] / tt[k];
+      D = D + w;
+      Nx = Nx + w * ox[k]; Ny = Ny + w * oy[k]; Nz = Nz + w * oz[k];
+      ca.q0[kd] = tt[k] / (tt[k] + tau);
+      ca.q1[kd] = tau / (tt[k] + tau);
+    }
+    ca.q0[kg] = 1.0 / (tau * D);
+    ca.q1[kg] = 1.0 / D;
+    ca.a0[kg] = Nx; ca.a1[kg] = Ny; ca.a2[kg] = Nz;
+  }
 }
 
+template <bool FAST>
 __global__ void k_idic_solve(const TubeDesc *tubes, const TubeState *tstate, const int *tube_cell0, int ntubes,
                              int ncell_total, CellArrays ca) {
   const int gc = blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,15 +361,16 @@ __global__ void k_idic_solve(const TubeDesc *tubes, const TubeState *tstate, con
   const int c = gc - tube_cell0[t];
   const double tau = tstate[t].dt;
   switch (T.n_dust) {
-    case 1: idic_solve_cell<1>(T, c, tau, ca); break;
-    case 2: idic_solve_cell<2>(T, c, tau, ca); break;
-    case 3: idic_solve_cell<3>(T, c, tau, ca); break;
-    default: idic_solve_cell<4>(T, c, tau, ca); break;
+    case 1: idic_solve_cell<1, FAST>(T, c, tau, ca); break;
+    case 2: idic_solve_cell<2, FAST>(T, c, tau, ca); break;
+    case 3: idic_solve_cell<3, FAST>(T, c, tau, ca); break;
+    default: idic_solve_cell<4, FAST>(T, c, tau, ca); break;
   }
 }
 
 // V_dustKernel_IDIC / V_gasKernel_IDIC (IDIC.h:264-315), MoveKernel_IDIC
 // (IDIC.h:319-333, periodic wrap as an extension), EnergyKernel_IDIC (335-346).
+template <bool FAST>
 __global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, const Chunk *chunks, int nchunks,
                              DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -311,6 +386,21 @@ __global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, con
     double vx = st.vx[i], vy = st.vy[i], vz = st.vz[i];
     if (cell < 0) {
       atomicOr(flags, 1);  // DS_FLAG_IDIC_RANGE: left unrelaxed
+    } else if (FAST) {
+      const int kg = T.idic_base[0] + cell;
+      if (s > 0) {
+        const int kd = T.idic_base[s] + cell;
+        const double a0 = ca.q0[kd], a1 = ca.q1[kd];
+        vx = a0 * vx + a1 * ca.nvx[kg];
+        vy = a0 * vy + a1 * ca.nvy[kg];
+        vz = a0 * vz + a1 * ca.nvz[kg];
+      } else {
+        const bool own = (T.mode & M_GAS_ACC_P) != 0;
+        const double a0 = ca.q0[kg], a1 = ca.q1[kg];
+        vx = a0 * vx + a1 * (ca.a0[kg] + (own ? st.ax[i] : ca.px[kg]));
+        vy = a0 * vy + a1 * (ca.a1[kg] + (own ? st.ay[i] : ca.py[kg]));
+        vz = a0 * vz + a1 * (ca.a2[kg] + (own ? st.az[i] : ca.pz[kg]));
+      }
     } else if (s > 0) {
       const int kg = T.idic_base[0] + cell, kd = T.idic_base[s] + cell;
       const double ts = ca.px[kd];
@@ -460,6 +550,50 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
   }
 }
 
+// Largest h of each cell (every key), for the stencil-radius choice.
+__global__ void k_cell_hmax(const int *cell_start, int nkeys, const double *h, double *hmax) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nkeys) return;
+  double m = 0.0;
+  for (int j = cell_start[k]; j < cell_start[k + 1]; j++) m = fmax(m, h[j]);
+  hmax[k] = m;
+}
+
+// Stencil radius each cell's force sweep needs: 1 when no particle within two
+// cells has h above half the cell width (every partner within the cut-off is
+// then in the 27 inner cells), else the tube's stencil.
+__global__ void k_cell_radius(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
+                              const int *nseg_species, int nseg, int nkeys, const double *hmax,
+                              unsigned char *krad) {
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  if (key >= nkeys) return;
+  const int sg = find_seg(nseg_key0, nseg, key);
+  const TubeDesc &T = tubes[nseg_tube[sg]];
+  const int kb = T.key_base[nseg_species[sg]];
+  const int local = key - kb;
+  if (T.stencil == 1) { krad[key] = 1; return; }
+  if (local >= T.ncells || !(T.mode & M_GRID_PROPER)) { krad[key] = (unsigned char)T.stencil; return; }
+  const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
+  const int R = T.stencil;
+  double H = 0.0;
+  for (int k = -R; k <= R; k++) {
+    const int cx = ix + k;
+    if (cx < 0 || cx >= T.nx) continue;
+    for (int l = -R; l <= R; l++) {
+      int cy = iy + l;
+      if (T.mode & M_PER_Y) cy = (cy + T.ny) % T.ny;
+      else if (cy < 0 || cy >= T.ny) continue;
+      for (int g = -R; g <= R; g++) {
+        int cz = iz + g;
+        if (T.mode & M_PER_Z) cz = (cz + T.nz) % T.nz;
+        else if (cz < 0 || cz >= T.nz) continue;
+        H = fmax(H, hmax[kb + cx + cy * T.sy + cz * T.sz]);
+      }
+    }
+  }
+  krad[key] = H <= T.r1_hmax ? 1 : (unsigned char)R;
+}
+
 __global__ void k_fill(double *a, int n, double v) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] = v;
@@ -481,34 +615,49 @@ void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cuda
   k_step_begin<<<blocks_for(ntubes, 64), 64, 0, s>>>(tubes, ts, ntubes);
 }
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                    uint32_t *vin, cudaStream_t s) {
-  if (nchunks) k_keys<<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
+                    uint32_t *vin, bool fast, cudaStream_t s) {
+  if (!nchunks) return;
+  if (fast) k_keys<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
+  else k_keys<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
 }
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
-                       DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local, uint32_t *ikin,
-                       uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, cudaStream_t s) {
-  if (nchunks)
-    k_reorder<<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, src, dst, pos32, vm32, idic_local, ikin,
-                                           ivin, slot_of_pid, ind_of_pid);
+                       const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
+                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, bool fast, cudaStream_t s) {
+  if (!nchunks) return;
+  if (fast)
+    k_reorder<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
+                                                 idic_local, ikin, ivin, slot_of_pid, ind_of_pid);
+  else
+    k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
+                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid);
 }
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s) {
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start);
 }
-void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
+void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
                            cudaStream_t s) {
-  if (n) k_idic_reduce<<<blocks_for(n, 256), 256, 0, s>>>(ikey, islot, n, seg_key0, seg_species, seg_orphan, nseg,
-                                                          st, ca);
+  if (nikeys <= 0) return;
+  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start);
+  k_idic_reduce<<<blocks_for(nikeys, 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st,
+                                                        ca);
 }
 void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
-                          int ncell_total, CellArrays ca, cudaStream_t s) {
-  if (ncell_total) k_idic_solve<<<blocks_for(ncell_total, 128), 128, 0, s>>>(tubes, ts, tube_cell0, ntubes,
-                                                                             ncell_total, ca);
+                          int ncell_total, CellArrays ca, bool fast, cudaStream_t s) {
+  if (!ncell_total) return;
+  if (fast)
+    k_idic_solve<true><<<blocks_for(ncell_total, 128), 128, 0, s>>>(tubes, ts, tube_cell0, ntubes, ncell_total, ca);
+  else
+    k_idic_solve<false><<<blocks_for(ncell_total, 128), 128, 0, s>>>(tubes, ts, tube_cell0, ntubes, ncell_total, ca);
 }
 void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
                           DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags,
-                          cudaStream_t s) {
-  if (nchunks) k_relax_move<<<nchunks, DS_CHUNK, 0, s>>>(tubes, ts, chunks, nchunks, st, idic_local, edot, ca, flags);
+                          bool fast, cudaStream_t s) {
+  if (!nchunks) return;
+  if (fast)
+    k_relax_move<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, ts, chunks, nchunks, st, idic_local, edot, ca, flags);
+  else
+    k_relax_move<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, ts, chunks, nchunks, st, idic_local, edot, ca, flags);
 }
 void ds_launch_tstop(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
                      const int *gas_slot_of_pid, int *flags, cudaStream_t s) {
@@ -534,4 +683,12 @@ void ds_launch_fill(double *a, int n, double v, cudaStream_t s) {
 }
 void ds_launch_iota(int *a, int n, cudaStream_t s) {
   if (n > 0) k_iota<<<blocks_for(n, 256), 256, 0, s>>>(a, n);
+}
+void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, const double *h,
+                           double *hmax, const int *nseg_key0, const int *nseg_tube, const int *nseg_species,
+                           int nseg, unsigned char *krad, cudaStream_t s) {
+  if (nkeys <= 0) return;
+  k_cell_hmax<<<blocks_for(nkeys, 256), 256, 0, s>>>(cell_start, nkeys, h, hmax);
+  k_cell_radius<<<blocks_for(nkeys, 128), 128, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys,
+                                                      hmax, krad);
 }

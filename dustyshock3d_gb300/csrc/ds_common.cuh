@@ -53,6 +53,10 @@ struct TubeDesc {
   double fx, fy, fz;
   float pre_abs;   // absolute slack of the FP32 distance prefilter
   int cellrel;
+  int stencil;       // cells searched on each side (1: 27 cells, 2: 125 cells)
+  int pad2;
+  double r1_hmax;    // particles and cells with h <= r1_hmax need only the 27 inner cells
+  double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
   // segments
   int seg_begin[DS_MAXS], seg_end[DS_MAXS];
   int key_base[DS_MAXS];   // neighbour keys of species s: key_base[s] + 0..ncells+1
@@ -173,10 +177,16 @@ __device__ __forceinline__ void ds_stencil_init(const TubeDesc &T, double x, dou
   }
 }
 
-// offset o = 0..26 -> local cell (or -1) and image shifts
-__device__ __forceinline__ int ds_stencil_cell(const TubeDesc &T, const Stencil &s, int o, double &shy,
-                                               double &shz) {
-  const int k = o / 9 - 1, l = (o / 3) % 3 - 1, g = o % 3 - 1;
+// Offset o of the (2r+1)^3 stencil, in the reference's launch order (k = x
+// offset outer, l = y, g = z inner): local cell (or -1), image shifts and the
+// cell offsets (k, l, g).  For r = 1 this is the reference's 27-offset loop;
+// the 27 inner offsets of r = 2 come in the same relative order.
+__device__ __forceinline__ int ds_stencil_cell(const TubeDesc &T, const Stencil &s, int r, int o, double &shy,
+                                               double &shz, int &k, int &l, int &g) {
+  const int w = 2 * r + 1;
+  k = o / (w * w) - r;
+  l = (o / w) % w - r;
+  g = o % w - r;
   shy = 0.0;
   shz = 0.0;
   if (!(T.mode & M_GRID_PROPER)) {
@@ -195,6 +205,119 @@ __device__ __forceinline__ int ds_stencil_cell(const TubeDesc &T, const Stencil 
   }
   if (cy < 0 || cy >= T.ny || cz < 0 || cz >= T.nz) return -1;
   return cx + cy * T.sy + cz * T.sz;
+}
+
+// FP32 shift that brings a neighbour cell's FP32 coordinates into ours:
+// whole cell widths when coordinates are cell-relative (this also applies the
+// periodic image), the image shift when they are tube-relative.  wf holds the
+// cell widths in FP32 so the shift costs no FP64 work.
+__device__ __forceinline__ void ds_pre_shift(const TubeDesc &T, const float3 &wf, int k, int l, int g, double shy,
+                                             double shz, float &sx, float &sy, float &sz) {
+  if (T.cellrel) {
+    sx = (float)k * wf.x;
+    sy = (float)l * wf.y;
+    sz = (float)g * wf.z;
+  } else {
+    sx = 0.0f;
+    sy = (float)shy;
+    sz = (float)shz;
+  }
+}
+
+// Image shifts of the neighbour cell at offsets (l, g) from the own cell.
+__device__ __forceinline__ void ds_wrap_shift(const TubeDesc &T, const Stencil &S, int l, int g, double &shy,
+                                              double &shz) {
+  shy = 0.0;
+  shz = 0.0;
+  if (!(T.mode & M_GRID_PROPER)) return;
+  if (T.mode & M_PER_Y) {
+    const int cy = S.iy + l;
+    shy = cy < 0 ? -T.Ly : (cy >= T.ny ? T.Ly : 0.0);
+  }
+  if (T.mode & M_PER_Z) {
+    const int cz = S.iz + g;
+    shz = cz < 0 ? -T.Lz : (cz >= T.nz ? T.Lz : 0.0);
+  }
+}
+
+// Offset code of a list entry: (k, l, g) in [-2, 2]^3 as (k+2)*25+(l+2)*5+(g+2),
+// increasing in the reference's visiting order for either stencil radius.
+__device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
+  k = o5 / 25 - 2;
+  l = (o5 / 5) % 5 - 2;
+  g = o5 % 5 - 2;
+}
+
+// Warp-synchronous neighbour walk with per-thread candidate lists.
+//
+// All 32 lanes run the same loops: over the stencil offsets (to the largest
+// stencil in the warp), and over each offset's cell in pieces of DS_PIECE
+// candidates (to the longest cell in the warp).  Each lane screens its own
+// candidates with a cheap FP32 test (`screen`) and appends survivors to its
+// column of the block's shared list (entry = offset code << 25 | slot).
+// When any lane's list could overflow, every lane runs `use(slot, offset
+// code)` over its entries, in visiting order, and the lists restart.  The
+// expensive pair work thus runs on dense lists with the warp converged,
+// instead of a warp idling while one lane meets a neighbour.  Lanes without a
+// particle (act false) take part with empty stencils.
+#define DS_SWEEP_THREADS 128
+#define DS_LIST_CAP 32
+#define DS_PIECE 8
+#define DS_OFS_SHIFT 25
+#define DS_SLOT_MASK ((1u << DS_OFS_SHIFT) - 1u)
+
+template <class Screen, class Use>
+__device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, bool act, int r, int kb,
+                                        const int *cell_start, uint32_t *lst, Screen screen, Use use) {
+  const unsigned FULL = 0xffffffffu;
+  const int w = 2 * r + 1;
+  const int nofs = act ? w * w * w : 0;
+  const int nofs_w = __reduce_max_sync(FULL, nofs);
+  const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
+  int n = 0;
+  auto flush = [&]() {
+    const int nw = __reduce_max_sync(FULL, n);
+    for (int t = 0; t < nw; t++)
+      if (t < n) {
+        const uint32_t e = lst[t * DS_SWEEP_THREADS];
+        use((int)(e & DS_SLOT_MASK), (int)(e >> DS_OFS_SHIFT));
+      }
+    n = 0;
+  };
+  for (int o = 0; o < nofs_w; o++) {
+    int j0 = 0, j1 = 0;
+    uint32_t code = 0;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    if (o < nofs) {
+      double shy, shz;
+      int k, l, g;
+      const int cell = ds_stencil_cell(T, S, r, o, shy, shz, k, l, g);
+      if (cell >= 0) {
+        j0 = cell_start[kb + cell];
+        j1 = cell_start[kb + cell + 1];
+      }
+      ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+      code = (uint32_t)((k + 2) * 25 + (l + 2) * 5 + (g + 2)) << DS_OFS_SHIFT;
+    }
+    const int len_w = __reduce_max_sync(FULL, j1 - j0);
+    for (int p0 = 0; p0 < len_w; p0 += DS_PIECE) {
+      if (__any_sync(FULL, n + DS_PIECE > DS_LIST_CAP)) flush();
+      // the piece's screens are independent: unrolled, their loads are in flight together
+      bool pass[DS_PIECE];
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++) {
+        const int j = j0 + p0 + t;
+        pass[t] = (p0 + t < len_w) && (j < j1) && screen(j, sx, sy, sz);
+      }
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++)
+        if (pass[t]) {
+          lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t);
+          n++;
+        }
+    }
+  }
+  flush();
 }
 
 // neighbour coordinate (with its image shift) minus ours, as the oracle does
@@ -217,6 +340,8 @@ struct SweepArgs {
   double *pt64;             // p / (rho rho) per gas slot     -- written by density
   double *edot;             // energy rate per gas slot
   int *ncand, *nnb;         // optional counts (parity hook), indexed by slot
+  const uint32_t *skey;        // sorted neighbour key of each slot
+  const unsigned char *krad;   // stencil radius each cell's force sweep needs
   const int *gas_slot_of_pid;  // slot of gas particle pid (index coupling)
   const int *gas_ind_pid;      // gas Ind by pid (index-coupled dust rho zeroing)
   TubeState *tstate_rw;

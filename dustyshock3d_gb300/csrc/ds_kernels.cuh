@@ -16,23 +16,27 @@ struct CellArrays {
   double *a0, *a1, *a2;     // gas: sums of A; dust: a0 = sum of t_stop
   double *nvx, *nvy, *nvz;  // solved cell velocities
   double *px, *py, *pz;     // gas: Psi; dust: px = mean t_stop, py = eps
+  double *q0, *q1;          // FP32 path: relax coefficients (v_new = q0 v + q1 (...))
+  int *start;               // first sorted IDIC slot of every key (run bounds)
 };
 
 void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
+// fast: FP32 path (reciprocal-multiply cell indices, slot-order scatters);
+// otherwise the reference's divisions and caller-index order.
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                    uint32_t *vin, cudaStream_t s);
+                    uint32_t *vin, bool fast, cudaStream_t s);
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
-                       DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local, uint32_t *ikin,
-                       uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, cudaStream_t s);
+                       const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
+                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, bool fast, cudaStream_t s);
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s);
-void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, const int *seg_key0,
+void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
                            cudaStream_t s);
 void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
-                          int ncell_total, CellArrays ca, cudaStream_t s);
+                          int ncell_total, CellArrays ca, bool fast, cudaStream_t s);
 void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
                           DevState st, const int *idic_local, const double *edot, CellArrays ca, int *flags,
-                          cudaStream_t s);
+                          bool fast, cudaStream_t s);
 void ds_launch_tstop(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
                      const int *gas_slot_of_pid, int *flags, cudaStream_t s);
 void ds_launch_dt(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
@@ -41,6 +45,9 @@ void ds_launch_conservation(const TubeDesc *tubes, int tube, DevState st, double
 void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nseg_particles, int ncells,
                            DevState st, const int *cell_start, int *head, int *next, int *rawkey, cudaStream_t s);
 
+void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, const double *h,
+                           double *hmax, const int *nseg_key0, const int *nseg_tube, const int *nseg_species,
+                           int nseg, unsigned char *krad, cudaStream_t s);
 void ds_launch_fill(double *a, int n, double v, cudaStream_t s);
 void ds_launch_iota(int *a, int n, cudaStream_t s);
 

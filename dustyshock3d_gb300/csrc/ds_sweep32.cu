@@ -1,7 +1,7 @@
 // ds_sweep32.cu -- FP32 neighbour sweeps with Kahan-compensated sums.
 //
-// Same traversal as ds_sweep64.cu (27 cells in the reference's order, one
-// thread per particle), but every per-pair quantity is FP32: positions are FP32
+// Same traversal as ds_sweep64.cu (stencil cells in the reference's order,
+// one thread per particle, screened candidates listed in shared memory), but every per-pair quantity is FP32: positions are FP32
 // offsets from the particle's own cell origin (proper grid; a neighbour cell's
 // offsets are shifted by whole cell widths, which also applies the periodic
 // image), velocities/masses come from packed float4 copies, and each sum is
@@ -47,68 +47,54 @@ __device__ __forceinline__ float dw_shape(float q) {
   return 0.0f;
 }
 
-__device__ __forceinline__ void cell_shift(const TubeDesc &T, int o, double shy, double shz, float &sx, float &sy,
-                                           float &sz) {
-  if (T.cellrel) {
-    const int k = o / 9 - 1, l = (o / 3) % 3 - 1, g = o % 3 - 1;
-    sx = (float)(k * T.wx);
-    sy = (float)(l * T.wy);
-    sz = (float)(g * T.wz);
-  } else {
-    sx = 0.0f;
-    sy = (float)shy;
-    sz = (float)shz;
-  }
-}
-
 template <bool HPP, int WHAT>
-__global__ void __launch_bounds__(DS_CHUNK) k_density32(SweepArgs a) {
-  const float c_pi = 1.0f / 3.14159265f;
-  (void)c_pi;
+__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
+  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
-    if (i >= ch.end) continue;
-    if (!a.tstate[ch.tube].active) continue;
+    const bool valid = i < ch.end && a.tstate[ch.tube].active;
     const TubeDesc &T = a.tubes[ch.tube];
     const int s = ch.species;
-    const int ind = a.st.ind[i];
-    const bool upd = ind == 0;
+    const int ind = valid ? a.st.ind[i] : 1;
+    const bool upd = valid && ind == 0;
     bool zero = upd;
-    if (WHAT == 1 && (T.mode & M_REF_COUPLING)) {
+    if (valid && WHAT == 1 && (T.mode & M_REF_COUPLING)) {
       const int q = a.st.pid[i];
       const int ng = T.seg_end[0] - T.seg_begin[0];
       zero = q < ng && a.gas_ind_pid[T.seg_begin[0] + q] == 0;
     }
-    double rho = a.st.rho[i];
+    double rho = valid ? a.st.rho[i] : 0.0;
     if (zero) rho = 0.0;
-    if (upd) {
-      const double xi = a.st.x[i], yi = a.st.y[i], zi = a.st.z[i];
-      const double hd = HPP ? a.st.h[i] : T.h;
-      const float4 pi = a.pos32[i];
-      const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
-      Stencil S;
-      ds_stencil_init(T, xi, yi, zi, S);
-      const int kb = T.key_base[s];
-      Kahan sum;
-      for (int o = 0; o < 27; o++) {
-        double shy, shz;
-        const int cell = ds_stencil_cell(T, S, o, shy, shz);
-        if (cell < 0) continue;
-        float sx, sy, sz;
-        cell_shift(T, o, shy, shz, sx, sy, sz);
-        const int j1 = a.cell_start[kb + cell + 1];
-        for (int j = a.cell_start[kb + cell]; j < j1; j++) {
+    const double xi = upd ? a.st.x[i] : 0.0, yi = upd ? a.st.y[i] : 0.0, zi = upd ? a.st.z[i] : 0.0;
+    const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
+    const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
+    const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
+    Stencil S;
+    ds_stencil_init(T, xi, yi, zi, S);
+    const int r = hd <= T.r1_hmax ? 1 : T.stencil;
+    Kahan sum;
+    ds_walk(
+        T, S, upd, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+        [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
           const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          if (r2 >= cut2) continue;
-          sum.add(a.vm32[j].w * w_shape(sqrtf(r2) * inv_h));
-        }
-      }
-      const double norm = ((double)1 / (DS_PI_REF)) / (hd * hd * hd);
-      rho = rho + norm * sum.value();
-    }
+          return dx * dx + dy * dy + dz * dz < cut2;
+        },
+        [&](int j, int o5) {
+          int k, l, g;
+          ds_decode_ofs(o5, k, l, g);
+          double shy, shz;
+          ds_wrap_shift(T, S, l, g, shy, shz);
+          float sx, sy, sz;
+          ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+          const float4 pj = a.pos32[j];
+          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          sum.add(a.vm32[j].w * w_shape(sqrtf(dx * dx + dy * dy + dz * dz) * inv_h));
+        });
+    if (!valid) continue;
+    if (upd) rho = rho + (((double)1 / (DS_PI_REF)) / (hd * hd * hd)) * sum.value();
     if (zero || upd) a.st.rho[i] = rho;
     if (WHAT == 0) {
       double p = a.st.p[i];
@@ -116,87 +102,90 @@ __global__ void __launch_bounds__(DS_CHUNK) k_density32(SweepArgs a) {
         p = ds_eq_state(rho, a.st.e[i], T.type_of_state, T.gam, T.cs);
         a.st.p[i] = p;
       }
-      const double cs = sqrt(T.gam * p / rho);
-      const double pt = p / (rho * rho);
-      a.cs64[i] = cs;
-      a.pt64[i] = pt;
-      a.hyd32[i] = make_float4((float)cs, (float)pt, (float)rho, 0.0f);
+      // force inputs and the CFL bound in FP32 (the force sweep is FP32)
+      const float rhof = (float)rho, pf = (float)p;
+      const float csf = sqrtf((float)T.gam * pf / rhof);
+      a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 0.0f);
       if (upd && (T.mode & M_CFL)) {
-        const double vx = a.st.vx[i], vy = a.st.vy[i], vz = a.st.vz[i];
-        const double v = sqrt(vx * vx + vy * vy + vz * vz);
-        const double hh = HPP ? a.st.h[i] : T.h;
-        const double dt = hh / (cs + v);
-        atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong(dt));
+        const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
+        const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
+        atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong((double)dt));
       }
     }
   }
 }
 
 template <bool HPP>
-__global__ void __launch_bounds__(DS_CHUNK) k_force32(SweepArgs a) {
+__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
+  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
   const float c_pi = (float)(1.0 / 3.14159265);
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
-    if (i >= ch.end) continue;
-    if (!a.tstate[ch.tube].active) continue;
-    if (a.st.ind[i] != 0) continue;
     const TubeDesc &T = a.tubes[ch.tube];
+    const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int s = ch.species;
-    const double xi = a.st.x[i], yi = a.st.y[i], zi = a.st.z[i];
-    const float4 pi = a.pos32[i];
-    const float4 vmi = a.vm32[i];
-    const float4 hyi = a.hyd32[i];
+    const double xi = act ? a.st.x[i] : 0.0, yi = act ? a.st.y[i] : 0.0, zi = act ? a.st.z[i] : 0.0;
+    const float4 pi = act ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 1.f);
+    const float4 vmi = act ? a.vm32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 hyi = act ? a.hyd32[i] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float hi = HPP ? pi.w : (float)T.h;
     const float inv_hi = 1.0f / hi;
     const float ni = c_pi * inv_hi * inv_hi * inv_hi * inv_hi;
     const float mi = vmi.w, rhoi = hyi.z, pti = hyi.y, csi = hyi.x;
-    const float mpi = (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i]));
+    const float mpi = act ? (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i])) : 0.0f;
     const float alpha = (float)T.alpha, beta = (float)T.beta, eps = (float)T.eps;
+    const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
     Kahan Ax, Ay, Az, et;
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
-    const int kb = T.key_base[s];
-    for (int o = 0; o < 27; o++) {
-      double shy, shz;
-      const int cell = ds_stencil_cell(T, S, o, shy, shz);
-      if (cell < 0) continue;
-      float sx, sy, sz;
-      cell_shift(T, o, shy, shz, sx, sy, sz);
-      const int j1 = a.cell_start[kb + cell + 1];
-      for (int j = a.cell_start[kb + cell]; j < j1; j++) {
-        const float4 pj = a.pos32[j];
-        const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        const float hj = HPP ? pj.w : hi;
-        const float hc = HPP ? fmaxf(hi, hj) : hi;
-        if (!(r2 < 4.0f * hc * hc) || !(r2 > 0.0f)) continue;
-        const float dist = sqrtf(r2);
-        const float inv_d = 1.0f / dist;
-        const float4 vmj = a.vm32[j];
-        const float4 hyj = a.hyd32[j];
-        const float hh = HPP ? 0.5f * (hi + hj) : hi;
-        const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
-        float F = 0.0f;
-        if (nu < 0.0f) {
-          const float Cnu = 0.5f * (csi + hyj.x);
-          const float mu = hh * nu / (r2 + eps * hh * hh);
-          F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
-        }
-        float dWr = ni * dw_shape(dist * inv_hi);
-        if (HPP) {
-          const float inv_hj = 1.0f / hj;
-          const float nj = c_pi * inv_hj * inv_hj * inv_hj * inv_hj;
-          dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
-        }
-        const float gd = dWr * inv_d;
-        et.add((mpi + mi * F * 0.5f) * nu * gd);
-        const float A = vmj.w * (pti + hyj.y + F) * gd;
-        Ax.add(dx * A);
-        Ay.add(dy * A);
-        Az.add(dz * A);
-      }
-    }
+    const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
+    ds_walk(
+        T, S, act, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+        [&](int j, float sx, float sy, float sz) {
+          const float4 pj = a.pos32[j];
+          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const float hc = HPP ? fmaxf(hi, pj.w) : hi;
+          return (r2 < 4.0f * hc * hc) && (r2 > 0.0f);
+        },
+        [&](int j, int o5) {
+          int k, l, g;
+          ds_decode_ofs(o5, k, l, g);
+          double shy, shz;
+          ds_wrap_shift(T, S, l, g, shy, shz);
+          float sx, sy, sz;
+          ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+          const float4 pj = a.pos32[j];
+          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const float inv_d = rsqrtf(r2);
+          const float dist = r2 * inv_d;
+          const float hj = HPP ? pj.w : hi;
+          const float4 vmj = a.vm32[j];
+          const float4 hyj = a.hyd32[j];
+          const float hh = HPP ? 0.5f * (hi + hj) : hi;
+          const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
+          float F = 0.0f;
+          if (nu < 0.0f) {
+            const float Cnu = 0.5f * (csi + hyj.x);
+            const float mu = hh * nu / (r2 + eps * hh * hh);
+            F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
+          }
+          float dWr = ni * dw_shape(dist * inv_hi);
+          if (HPP) {
+            const float inv_hj = 1.0f / hj;
+            const float nj = c_pi * inv_hj * inv_hj * inv_hj * inv_hj;
+            dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
+          }
+          const float gd = dWr * inv_d;
+          et.add((mpi + mi * F * 0.5f) * nu * gd);
+          const float A = vmj.w * (pti + hyj.y + F) * gd;
+          Ax.add(dx * A);
+          Ay.add(dy * A);
+          Az.add(dz * A);
+        });
+    if (!act) continue;
     a.st.ax[i] = Ax.value();
     a.st.ay[i] = Ay.value();
     a.st.az[i] = Az.value();
@@ -209,16 +198,16 @@ __global__ void __launch_bounds__(DS_CHUNK) k_force32(SweepArgs a) {
 void ds_launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
   if (!a.nchunks) return;
   if (what == 0) {
-    if (hpp) k_density32<true, 0><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
-    else k_density32<false, 0><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+    if (hpp) k_density32<true, 0><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_density32<false, 0><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
   } else {
-    if (hpp) k_density32<true, 1><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
-    else k_density32<false, 1><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+    if (hpp) k_density32<true, 1><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_density32<false, 1><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
   }
 }
 
 void ds_launch_force32(const SweepArgs &a, bool hpp, cudaStream_t s) {
   if (!a.nchunks) return;
-  if (hpp) k_force32<true><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
-  else k_force32<false><<<a.nchunks, DS_CHUNK, 0, s>>>(a);
+  if (hpp) k_force32<true><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  else k_force32<false><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
 }

@@ -202,7 +202,7 @@ def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0
                Maximum_particle=gas.n, Particle_on_length=1.0 / dx_left, h=h_max, Coeff_h_dust_cell=0.5,
                tau=fixed_tau if fixed_tau else 1e-4, T_end=t_end, T_out=t_end, alpha=alpha, beta=beta,
                eps=av_eps, Gam_g=gamma, Speed_of_sound_gas=1.0, n_dust=1, mass_ratio=[eps], R_dust=[0.0],
-               t_stop_const=[t_s], eps_empty=[eps], t_empty=t_s, cell_w=2.0 * h_max,
+               t_stop_const=[t_s], eps_empty=[eps], t_empty=t_s, cell_w=1.001 * h_max, stencil=2,
                idic_w=idic_cells_per_right_spacing * R["dx"], cfl=cfl, mode=Mode.baseline())
     if fixed_tau:
         P.mode.cfl = False

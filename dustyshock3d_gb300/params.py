@@ -93,6 +93,7 @@ class Params:
     cell_w: float = 0.0   # neighbour cell width; 0 -> 2h (kernel.cu:1773)
     idic_w: float = 0.0   # IDIC cell width; 0 -> Coeff_h_dust_cell * h (kernel.cu:1577)
     cfl: float = 0.3
+    stencil: int = 1      # cells searched on each side: 1 (the reference's 27 cells) or 2 (125 cells)
     precision: str = "fp64"  # "fp64" or "fp32" (FP32 neighbour sums, FP64 state/IDIC)
     mode: Mode = field(default_factory=Mode)
 
@@ -153,8 +154,8 @@ def parse_init_txt(text: str) -> Params:
             setattr(P.mode, key[5:], val.lower() in ("1", "true", "yes", "on"))
         elif key in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             setattr(P, key, [float(v) for v in val.replace(",", " ").split()])
-        elif key in ("n_dust",):
-            P.n_dust = int(val)
+        elif key in ("n_dust", "stencil"):
+            setattr(P, key, int(val))
         elif key == "precision":
             P.precision = val
         elif hasattr(P, key):
@@ -178,6 +179,7 @@ def write_init_txt(P: Params, extensions: bool = True) -> str:
         for k in ("Gam_g", "Speed_of_sound_gas", "t_empty", "cell_w", "idic_w", "cfl"):
             out.append(f"{k} = {getattr(P, k)!r}")
         out.append(f"n_dust = {P.n_dust}")
+        out.append(f"stencil = {P.stencil}")
         for k in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             out.append(f"{k} = " + " ".join(repr(float(v)) for v in getattr(P, k)))
         out.append(f"precision = {P.precision}")

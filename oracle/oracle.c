@@ -166,30 +166,34 @@ static void orc_list(const orc_grid *G, const orc_species *s, int *head, int *ne
   }
 }
 
-/* The 27 neighbour cells of particle i in the reference's launch order
- * (k = x offset outer, l = y, g = z inner; kernel.cu:2014-2016) with the
- * validity test of IDIC.h:30-31.  Proper grid: same order, per-axis range
- * checks, periodic wrap with image shifts.  Invalid offsets get cell -1. */
-typedef struct { int cell[27]; double sx[27], sy[27], sz[27]; } orc_stencil;
+/* The neighbour cells of a particle in the reference's launch order (k = x
+ * offset outer, l = y, g = z inner; kernel.cu:2014-2016) with the validity
+ * test of IDIC.h:30-31: 27 cells for stencil 1 (the reference), 125 for
+ * stencil 2 (extension: cells of half the width).  Proper grid: same order,
+ * per-axis range checks, periodic wrap with image shifts.  Invalid offsets
+ * get cell -1. */
+#define ORC_MAX_OFS 125
+typedef struct { int n; int cell[ORC_MAX_OFS]; double sx[ORC_MAX_OFS], sy[ORC_MAX_OFS], sz[ORC_MAX_OFS]; } orc_stencil;
 
-static void orc_make_stencil(const orc_grid *G, double x, double y, double z, orc_stencil *st) {
+static void orc_make_stencil(const orc_grid *G, int R, double x, double y, double z, orc_stencil *st) {
   int o = 0;
   if (!G->proper) {
     int Ni = orc_key(G, x, y, z);
-    for (int k = -1; k <= 1; k++)
-      for (int l = -1; l <= 1; l++)
-        for (int g = -1; g <= 1; g++, o++) {
+    for (int k = -R; k <= R; k++)
+      for (int l = -R; l <= R; l++)
+        for (int g = -R; g <= R; g++, o++) {
           int Ci = Ni + k + l * G->Cnx + g * G->Cnx * G->Cny;
           st->cell[o] = ((Ci > -1) && (Ci < G->ncells)) ? Ci : -1;
           st->sx[o] = st->sy[o] = st->sz[o] = 0.0;
         }
+    st->n = o;
     return;
   }
   int ix, iy, iz;
   orc_proper_cell(G, x, y, z, &ix, &iy, &iz);
-  for (int k = -1; k <= 1; k++)
-    for (int l = -1; l <= 1; l++)
-      for (int g = -1; g <= 1; g++, o++) {
+  for (int k = -R; k <= R; k++)
+    for (int l = -R; l <= R; l++)
+      for (int g = -R; g <= R; g++, o++) {
         int cx = ix + k, cy = iy + l, cz = iz + g;
         double sy = 0.0, sz = 0.0;
         int ok = (cx >= 0 && cx < G->nx);
@@ -205,6 +209,7 @@ static void orc_make_stencil(const orc_grid *G, double x, double y, double z, or
         st->cell[o] = ok ? cx + cy * G->sy + cz * G->sz : -1;
         st->sx[o] = 0.0; st->sy[o] = sy; st->sz[o] = sz;
       }
+  st->n = o;
 }
 
 /* Difference of a neighbour coordinate (with its image shift) and ours. */
@@ -219,13 +224,14 @@ static inline double orc_diff(double xj, double s, double xi) { return s != 0.0 
 static void orc_density(const orc_params *P, const orc_grid *G, orc_species *s, const int *head,
                         const int *next, const int *upd) {
   const int hpp = (P->flags & ORC_H_PER_PARTICLE) != 0;
+  const int R = P->stencil == 2 ? 2 : 1;
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < s->n; i++) {
     if (!upd[i]) continue;
     orc_stencil st;
-    orc_make_stencil(G, s->x[i], s->y[i], s->z[i], &st);
+    orc_make_stencil(G, R, s->x[i], s->y[i], s->z[i], &st);
     const double hi = hpp ? s->h[i] : P->h;
-    for (int o = 0; o < 27; o++) {
+    for (int o = 0; o < st.n; o++) {
       double rho_tmp = 0.0;
       if (st.cell[o] >= 0) {
         int j = head[st.cell[o]];
@@ -248,14 +254,15 @@ static void orc_density(const orc_params *P, const orc_grid *G, orc_species *s, 
 static void orc_force(const orc_params *P, const orc_grid *G, orc_species *s, const int *head,
                       const int *next, double *e_temp) {
   const int hpp = (P->flags & ORC_H_PER_PARTICLE) != 0;
+  const int R = P->stencil == 2 ? 2 : 1;
   const double Gam_g = P->Gam_g, alpha = P->alpha, beta = P->beta, eps = P->eps;
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < s->n; i++) {
     if (s->ind[i] != 0) continue;
     orc_stencil st;
-    orc_make_stencil(G, s->x[i], s->y[i], s->z[i], &st);
+    orc_make_stencil(G, R, s->x[i], s->y[i], s->z[i], &st);
     const double hi = hpp ? s->h[i] : P->h;
-    for (int o = 0; o < 27; o++) {
+    for (int o = 0; o < st.n; o++) {
       if (st.cell[o] < 0) continue;
       int j = head[st.cell[o]];
       while (j > -1) {
@@ -365,7 +372,10 @@ void orc_idic_solve_cell(int n, const double *eps, const double *t, double vg, c
 int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken) {
   orc_grid G;
   orc_grid_setup(P, &G);
-  if ((G.per_y && G.ny < 3) || (G.per_z && G.nz < 3)) return -1; /* periodic axis needs >= 3 cells */
+  {
+    const int need = 2 * (P->stencil == 2 ? 2 : 1) + 1; /* a periodic axis must not alias its own stencil */
+    if ((G.per_y && G.ny < need) || (G.per_z && G.nz < need)) return -1;
+  }
   const int nd = P->n_dust, ns = 1 + nd;
   orc_species *gas = &sp[0];
   const int Ng = gas->n;
@@ -641,6 +651,7 @@ void orc_neighbour_counts(const orc_params *P, const orc_species *s, int *ncand,
   orc_grid G;
   orc_grid_setup(P, &G);
   const int hpp = (P->flags & ORC_H_PER_PARTICLE) != 0;
+  const int R = P->stencil == 2 ? 2 : 1;
   int *head = (int *)malloc(sizeof(int) * (G.ncells + 1));
   int *next = (int *)malloc(sizeof(int) * (s->n > 0 ? s->n : 1));
   int *tail = (int *)malloc(sizeof(int) * (G.ncells + 1));
@@ -648,10 +659,10 @@ void orc_neighbour_counts(const orc_params *P, const orc_species *s, int *ncand,
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < s->n; i++) {
     orc_stencil st;
-    orc_make_stencil(&G, s->x[i], s->y[i], s->z[i], &st);
+    orc_make_stencil(&G, R, s->x[i], s->y[i], s->z[i], &st);
     const double hi = hpp ? s->h[i] : P->h;
     int nc = 0, nn = 0;
-    for (int o = 0; o < 27; o++) {
+    for (int o = 0; o < st.n; o++) {
       if (st.cell[o] < 0) continue;
       for (int j = head[st.cell[o]]; j > -1; j = next[j]) {
         nc++;

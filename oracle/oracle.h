@@ -52,7 +52,7 @@ typedef struct orc_params {
   double cfl;
   double t_empty;            /* empty-cell mean stopping time (kernel.cu:2160)       */
   int n_dust;
-  int pad_;
+  int stencil;               /* cells searched on each side: 1 (27 cells), 2 (125) */
   double mass_ratio[ORC_MAX_DUST];   /* mas_gas_dust_k (kernel.cu:1499-1502) */
   double R_dust[ORC_MAX_DUST];       /* R_dust_k                              */
   double t_stop_const[ORC_MAX_DUST]; /* extension: constant stopping time     */

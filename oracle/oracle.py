@@ -44,7 +44,7 @@ class OrcParams(ctypes.Structure):
         ("Gam_g", ctypes.c_double), ("Speed_of_sound_gas", ctypes.c_double),
         ("cell_w", ctypes.c_double), ("idic_w", ctypes.c_double),
         ("cfl", ctypes.c_double), ("t_empty", ctypes.c_double),
-        ("n_dust", ctypes.c_int), ("pad_", ctypes.c_int),
+        ("n_dust", ctypes.c_int), ("stencil", ctypes.c_int),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
         ("t_stop_const", ctypes.c_double * MAX_DUST), ("eps_empty", ctypes.c_double * MAX_DUST),
     ]
@@ -122,6 +122,7 @@ def to_orc_params(P) -> OrcParams:
     o.cell_w = float(P.cell_width())
     o.idic_w = float(P.idic_width())
     o.n_dust = int(P.n_dust)
+    o.stencil = int(getattr(P, "stencil", 1) or 1)
     f = 0
     m = P.mode
     if m.periodic_y: f |= ORC_PERIODIC_Y
@@ -186,7 +187,7 @@ class OracleState:
         for _ in range(n):
             st = L.orc_step(ctypes.byref(self.P), self._arr, ctypes.byref(Tm), ctypes.byref(dt))
             if st < 0:
-                raise ValueError("oracle: a periodic axis has fewer than 3 neighbour cells")
+                raise ValueError("oracle: a periodic axis has fewer cells than its stencil needs")
             self.last_status |= st
         self.Tm = Tm.value
         self.last_dt = dt.value
