@@ -75,7 +75,7 @@ struct ds_ctx {
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
-  double *cs64 = nullptr, *pt64 = nullptr, *edot = nullptr;
+  double *cs64 = nullptr, *pt64 = nullptr, *dwn64 = nullptr, *edot = nullptr;
   uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
   uint32_t *ikin = nullptr, *ivin = nullptr, *ikalt = nullptr, *ivalt = nullptr;
   uint32_t *rs_scratch = nullptr;
@@ -246,6 +246,7 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.hyd32 = c->hyd32;
   a.cs64 = c->cs64;
   a.pt64 = c->pt64;
+  a.dwn64 = c->dwn64;
   a.edot = c->edot;
   a.ncand = c->ncand;
   a.nnb = c->nnb;
@@ -386,7 +387,7 @@ ds_status finalize(ds_ctx *c) {
     DA(c->buf[b].pid, N);
   }
   DA(c->pos32, N); DA(c->vm32, N); DA(c->hyd32, N);
-  DA(c->cs64, N); DA(c->pt64, N); DA(c->edot, N);
+  DA(c->cs64, N); DA(c->pt64, N); DA(c->dwn64, N); DA(c->edot, N);
   DA(c->kin, N); DA(c->vin, N); DA(c->kalt, N); DA(c->valt, N);
   DA(c->ikin, N); DA(c->ivin, N); DA(c->ikalt, N); DA(c->ivalt, N);
   DA(c->rs_scratch, ds_radix_scratch_words(N));

@@ -112,6 +112,30 @@ __device__ __forceinline__ double ds_dW(double r, double h) {
   return c / (h * h * h * h) * tmp1;
 }
 
+// ds_dW with its normalisation c/(h*h*h*h) precomputed by the caller (the
+// same double, so the same result)
+__device__ __forceinline__ double ds_dW_n(double r, double h, double norm) {
+  double k = r / h, tmp1 = 0.0;
+  if ((k >= -2.0) && (k <= -1.0)) tmp1 = 0.75 * (2.0 + k) * (2.0 + k);
+  if ((k > -1.0) && (k < 0)) tmp1 = -3.0 * k - 2.25 * k * k;
+  if ((k >= 0) && (k <= 1.0)) tmp1 = -3.0 * k + 2.25 * k * k;
+  if ((k >= 1.0) && (k <= 2.0)) tmp1 = -0.75 * (2.0 - k) * (2.0 - k);
+  if ((k > 2.0) || (k < -2.0)) tmp1 = 0.0;
+  return norm * tmp1;
+}
+
+// ds_W with its normalisation c/(h*h*h) precomputed
+__device__ __forceinline__ double ds_W_n(double r, double h, double norm) {
+  double k = fabs(r) / h, tmp1 = 0.0;
+  if (k < 1.0) tmp1 = 1.0 - 1.5 * k * k + 0.75 * k * k * k;
+  if ((k >= 1.0) && (k <= 2.0)) tmp1 = 0.25 * (2.0 - k) * (2.0 - k) * (2.0 - k);
+  if (k > 2.0) tmp1 = 0.0;
+  return norm * tmp1;
+}
+
+__device__ __forceinline__ double ds_W_norm(double h) { return ((double)1 / (DS_PI_REF)) / (h * h * h); }
+__device__ __forceinline__ double ds_dW_norm(double h) { return ((double)1 / (DS_PI_REF)) / (h * h * h * h); }
+
 // kernel.cu:92-97
 __device__ __forceinline__ double ds_eq_state(double rho, double e, int type, double gam, double cs) {
   if (type == 1) return cs * cs * rho;
@@ -266,7 +290,7 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 #define DS_OFS_SHIFT 25
 #define DS_SLOT_MASK ((1u << DS_OFS_SHIFT) - 1u)
 
-template <class Screen, class Use>
+template <int CAP = DS_LIST_CAP, class Screen, class Use>
 __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, bool act, int r, int kb,
                                         const int *cell_start, uint32_t *lst, Screen screen, Use use) {
   const unsigned FULL = 0xffffffffu;
@@ -301,7 +325,7 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
     }
     const int len_w = __reduce_max_sync(FULL, j1 - j0);
     for (int p0 = 0; p0 < len_w; p0 += DS_PIECE) {
-      if (__any_sync(FULL, n + DS_PIECE > DS_LIST_CAP)) flush();
+      if (__any_sync(FULL, n + DS_PIECE > CAP)) flush();
       // the piece's screens are independent: unrolled, their loads are in flight together
       bool pass[DS_PIECE];
 #pragma unroll
@@ -338,6 +362,7 @@ struct SweepArgs {
   float4 *hyd32;            // FP32 c, p/rho^2, rho, (unused) -- written by density
   double *cs64;             // sqrt(gam p / rho) per gas slot -- written by density
   double *pt64;             // p / (rho rho) per gas slot     -- written by density
+  double *dwn64;            // dW normalisation c/h^4 per gas slot -- written by density
   double *edot;             // energy rate per gas slot
   int *ncand, *nnb;         // optional counts (parity hook), indexed by slot
   const uint32_t *skey;        // sorted neighbour key of each slot

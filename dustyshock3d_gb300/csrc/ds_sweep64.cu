@@ -37,8 +37,12 @@ __device__ __forceinline__ float pre_cut2(float two_h, float slack) {
 
 // what: 0 gas density + EOS + per-particle force inputs, 1 dust self-density.
 template <bool HPP, int WHAT>
+// FP64 pair work is heavy, so the lists are longer: flushes are rarer and the
+// lanes' lists are fuller when they run.
+#define DS_LIST_CAP64 64
+
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
-  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
+  __shared__ uint32_t lst[DS_LIST_CAP64 * DS_SWEEP_THREADS];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
@@ -65,7 +69,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
     const int r = hi <= T.r1_hmax ? 1 : T.stencil;
     double rho_tmp = 0.0;
     int cur_o = -1;
-    ds_walk(
+    const double wn = ds_W_norm(hi);
+    ds_walk<DS_LIST_CAP64>(
         T, S, upd, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
@@ -87,7 +92,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
           const double dy = ds_diff(a.st.y[j], shy, yi);
           const double dz = ds_diff(a.st.z[j], shz, zi);
           const double d = sqrt(dx * dx + dy * dy + dz * dz);
-          rho_tmp = rho_tmp + a.st.m[j] * ds_W(d, hi);
+          rho_tmp = rho_tmp + a.st.m[j] * ds_W_n(d, hi, wn);
         });
     rho = rho + rho_tmp;
     if (!valid) continue;
@@ -103,6 +108,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
       const double pt = p / (rho * rho);
       a.cs64[i] = cs;
       a.pt64[i] = pt;
+      a.dwn64[i] = ds_dW_norm(HPP ? a.st.h[i] : T.h);
       a.hyd32[i] = make_float4((float)cs, (float)pt, (float)rho, 0.0f);
       if (upd && (T.mode & M_CFL)) {
         const double vx = a.st.vx[i], vy = a.st.vy[i], vz = a.st.vz[i];
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
 // EnergyInitKernel_IDIC).
 template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force64(SweepArgs a) {
-  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
+  __shared__ uint32_t lst[DS_LIST_CAP64 * DS_SWEEP_THREADS];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
@@ -140,7 +146,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force64(SweepArgs a) {
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
     const float hif = (float)hi;
-    ds_walk(
+    const double dni = act ? a.dwn64[i] : 0.0;
+    ds_walk<DS_LIST_CAP64>(
         T, S, act, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
@@ -176,7 +183,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force64(SweepArgs a) {
             nu_temp = hh * nu_temp / (dist * dist + eps * hh * hh);
             F_nu = (-alpha * Cnu * nu_temp + beta * nu_temp * nu_temp) / (0.5 * (rhoi + rhoj));
           }
-          const double dWr = HPP ? 0.5 * (ds_dW(dist, hi) + ds_dW(dist, hj)) : ds_dW(dist, hi);
+          const double dWr =
+              HPP ? 0.5 * (ds_dW_n(dist, hi, dni) + ds_dW_n(dist, hj, a.dwn64[j])) : ds_dW_n(dist, hi, dni);
           et = et + (mpi + mi * F_nu / 2.0) * (nu1x + nu1y + nu1z) * dWr / dist;
           const double A = a.st.m[j] * (pti + a.pt64[j] + F_nu) * dWr;
           Ax = Ax + dxj * A / dist;
