@@ -25,6 +25,7 @@ cannot be built on the GPU host from this repository).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -35,6 +36,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+# Batched and served workloads (not the default line): 64 seeded uneven tubes,
+# and a Poisson stream of such tubes under a 150 GB budget.
+EXTRA_WORKLOADS = ("batch64", "serve")
 
 WORKLOADS = {
     # name: (dx_left, Ly, description)
@@ -52,7 +57,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + list(EXTRA_WORKLOADS))
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--rate", type=float, default=4.0, help="serve: mean arrivals per second")
+    ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -408,10 +416,93 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """64 uneven tubes (seeded) advanced together, FP32, autotuned."""
+    from dustyshock3d_gb300 import ic, tune
+    from dustyshock3d_gb300.solver import Solver
+    tubes = ic.batch_tubes(seed=args.seed, n_tubes=64)
+    choice, log = tune.tune(tubes, sample=8)
+    ps = []
+    for P, _ in tubes:
+        Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth)
+        Q.precision = "fp32"
+        ps.append(Q)
+    n = sum(sum(s.n for s in sp) for _, sp in tubes)
+    clocks = ClockSampler(0)
+    clocks.start()
+    with Solver(ps) as S:
+        for t, (_, sp) in enumerate(tubes):
+            S.set_tube(t, sp)
+        S.step(args.warmup)
+        total_ms, phase = S.step_timed(args.steps)
+        kps = S.kernels_per_step()
+        mem = S.memory_bytes()
+    clk = clocks.stop()
+    value = n * args.steps / (total_ms * 1e-3)
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64", "tubes": 64, "particles": n, "seed": args.seed,
+                       "autotuned": dataclasses.asdict(choice),
+                       "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, ms=d) for a, b, c, d in log],
+                       "device_bytes": mem},
+            "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
+                                                                     phase)},
+            "gpu_launches": kps * args.steps, "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
+def run_serve(args):
+    """Poisson stream of uneven tubes, continuous batching under 150 GB."""
+    import numpy as np
+
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300.serve import Server, poisson_requests
+    from dustyshock3d_gb300.solver import Solver
+    make = lambda rng: ic.uneven_tube(**ic.draw_tube_params(rng))  # noqa: E731
+    reqs = poisson_requests(args.rate, args.requests, args.seed, make)
+    clocks = ClockSampler(0)
+    clocks.start()
+    server = Server(budget_bytes=150e9, epoch_steps=10, precision="fp32")
+    t0 = time.perf_counter()
+    res = server.run(reqs)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    tts = np.array([r.time_to_solution for r in res])
+    ps = sum(r.particles * r.steps for r in res)
+    # the same requests one at a time on the plain FP64 path: FP64 rate measured on
+    # the median-size request (a few steps), applied to every request's work
+    mid = sorted(reqs, key=lambda r: r.particles)[len(reqs) // 2]
+    P = mid.params.copy()
+    P.T_end = 1e9
+    with Solver(P) as S:
+        S.set_tube(0, mid.species)
+        S.step(2)
+        ms, _ = S.step_timed(3)
+    fp64_rate = mid.particles * 3 / (ms * 1e-3)
+    line = {"metric": "particle-steps/s", "value": ps / wall, "unit": "particle-steps/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serve", "requests": len(reqs), "rate_per_s": args.rate, "seed": args.seed,
+                       "budget_bytes": 150e9, "epoch_steps": 10, "t_end": "U[0.05, 0.2]"},
+            "p50_time_to_solution_s": float(np.percentile(tts, 50)),
+            "p99_time_to_solution_s": float(np.percentile(tts, 99)), "wall_s": wall,
+            "rebuilds": server.rebuilds, "particle_steps": ps,
+            "one_at_a_time_fp64_estimate": {"rate": fp64_rate, "wall_s": ps / fp64_rate,
+                                            "sample": f"request {mid.rid} ({mid.particles} particles), 3 steps"},
+            "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

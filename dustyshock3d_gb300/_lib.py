@@ -33,7 +33,7 @@ class DsParams(ctypes.Structure):
         ("Gam_g", ctypes.c_double), ("Speed_of_sound_gas", ctypes.c_double),
         ("n_dust", ctypes.c_int), ("mode", ctypes.c_int), ("precision", ctypes.c_int), ("stencil", ctypes.c_int),
         ("cell_w", ctypes.c_double), ("idic_w", ctypes.c_double), ("cfl", ctypes.c_double),
-        ("t_empty", ctypes.c_double),
+        ("t_empty", ctypes.c_double), ("list_depth", ctypes.c_int), ("reserved1", ctypes.c_int),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
         ("t_stop_const", ctypes.c_double * MAX_DUST), ("eps_empty", ctypes.c_double * MAX_DUST),
     ]
@@ -51,6 +51,7 @@ SIGNATURES = {
     "ds_create_batch": ([ctypes.c_int, ctypes.POINTER(DsParams), ctypes.POINTER(_VP)], ctypes.c_int),
     "ds_set_gas": ([_VP, ctypes.c_int, ctypes.c_int] + [_DP] * 14 + [_IP], ctypes.c_int),
     "ds_set_dust": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [_DP] * 10 + [_IP], ctypes.c_int),
+    "ds_copy_tube": ([_VP, ctypes.c_int, _VP, ctypes.c_int], ctypes.c_int),
     "ds_upload_gas": ([_VP, ctypes.c_int] + [_DP] * 14 + [_IP], ctypes.c_int),
     "ds_upload_dust": ([_VP, ctypes.c_int, ctypes.c_int] + [_DP] * 10 + [_IP], ctypes.c_int),
     "ds_step": ([_VP, ctypes.c_int], ctypes.c_int),
@@ -118,6 +119,7 @@ def params_to_c(P: Params) -> DsParams:
     c.mode = mode
     c.precision = 1 if str(P.precision).lower() in ("fp32", "1") else 0
     c.stencil = int(getattr(P, "stencil", 1) or 1)
+    c.list_depth = int(getattr(P, "list_depth", 0) or 0)
     for k in range(MAX_DUST):
         c.mass_ratio[k] = float(P.mass_ratio[k]) if k < len(P.mass_ratio) else 0.0
         c.R_dust[k] = float(P.R_dust[k]) if k < len(P.R_dust) else 0.0

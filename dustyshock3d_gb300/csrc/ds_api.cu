@@ -53,6 +53,7 @@ struct ds_ctx {
   int ntubes = 0;
   std::vector<ds_params> params;
   std::vector<std::vector<HostSpecies>> host;  // [tube][species]
+  std::vector<std::pair<ds_ctx *, int>> dev_src;  // per tube: resident tube to copy from (ds_copy_tube)
   bool finalized = false;
   std::string msg;
   // sizes
@@ -215,6 +216,8 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
   if (T.ncells <= 0 || T.ncells > (1 << 28)) return fail(c, DS_ERR_ARG, "neighbour grid too large");
   if (T.n_idic <= 0 || T.n_idic > (1 << 28)) return fail(c, DS_ERR_ARG, "IDIC grid too large");
   if (P.stencil != 0 && P.stencil != 1 && P.stencil != 2) return fail(c, DS_ERR_ARG, "stencil must be 1 or 2");
+  if (P.list_depth != 0 && P.list_depth != 32 && P.list_depth != 64)
+    return fail(c, DS_ERR_ARG, "list_depth must be 0, 32 or 64");
   if (P.stencil == 2 && !(P.mode & DS_MODE_GRID_PROPER))
     return fail(c, DS_ERR_UNSUPPORTED, "stencil 2 needs the proper cell grid (DS_MODE_GRID_PROPER)");
   const int need = 2 * T.stencil + 1;  // a periodic axis must not alias its own stencil
@@ -292,17 +295,18 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
   const bool fp32 = c->any_fp32;
   SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
   SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
-  if (fp32) ds_launch_density32(ag, c->any_hpp, 0, s);
+  const int depth = c->params[0].list_depth;
+  if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
   if (c->any_dust_rho) {
-    if (fp32) ds_launch_density32(ad, c->any_hpp, 1, s);
+    if (fp32) ds_launch_density32(ad, c->any_hpp, 1, depth, s);
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
   }
   DevState st = c->buf[c->parity].view();
   ds_launch_tstop(c->d_tubes, c->d_tstate, c->d_ch_dust, (int)c->ch_dust.size(), st, c->slot_of_pid, c->d_flags, s);
   ds_launch_dt(c->d_tubes, c->d_tstate, c->ntubes, s);
   if (ev) cudaEventRecord(ev[2], s);
-  if (fp32) ds_launch_force32(ag, c->any_hpp, s);
+  if (fp32) ds_launch_force32(ag, c->any_hpp, depth, s);
   else ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
   if (ev) cudaEventRecord(ev[3], s);
   const uint32_t *ik = alt ? c->ikalt : c->ikin;
@@ -365,7 +369,10 @@ ds_status finalize(ds_ctx *c) {
     if (T.stencil == 2) c->any_stencil2 = true;
   }
   if (nkeys >= (1LL << 31) || nikeys >= (1LL << 31)) return fail(c, DS_ERR_ARG, "key space too large");
-  if (N >= (1 << 25)) return fail(c, DS_ERR_UNSUPPORTED, "more than 2^25 particles in one context");
+  for (const auto &T : c->tdesc)
+    for (int s = 0; s < DS_MAXS; s++)
+      if (T.seg_end[s] - T.seg_begin[s] >= (1 << 25))
+        return fail(c, DS_ERR_UNSUPPORTED, "more than 2^25 particles in one species of a tube");
   // one kernel variant per batch: the mode bits that select templates must agree
   for (int t = 1; t < c->ntubes; t++) {
     const ds_params &P = c->params[t];
@@ -430,6 +437,7 @@ ds_status finalize(ds_ctx *c) {
   c->parity = 0;
   for (int t = 0; t < c->ntubes; t++)
     for (int s = 0; s <= c->params[t].n_dust; s++) {
+      if (c->dev_src[t].first) continue;  // copied from a resident tube below
       HostSpecies &H = c->host[t][s];
       const int b = c->tdesc[t].seg_begin[s];
       for (int f = 0; f < NF; f++)
@@ -443,6 +451,24 @@ ds_status finalize(ds_ctx *c) {
       for (int f = 0; f < NF; f++) { std::vector<double>().swap(H.f[f]); }
       std::vector<int>().swap(H.ind);
     }
+  // tubes carried over from another context: state and clock, device to device
+  for (int t = 0; t < c->ntubes; t++) {
+    ds_ctx *src = c->dev_src[t].first;
+    if (!src) continue;
+    const int st_ = c->dev_src[t].second;
+    CK(cudaStreamSynchronize(src->stream));
+    const TubeDesc &S = src->tdesc[st_];
+    const Buffers &B = src->buf[src->parity];
+    for (int s = 0; s <= c->params[t].n_dust; s++) {
+      const int n = S.seg_end[s] - S.seg_begin[s], sb = S.seg_begin[s], db = c->tdesc[t].seg_begin[s];
+      if (n == 0) continue;
+      for (int f = 0; f < NF; f++)
+        CK(cudaMemcpyAsync(c->buf[0].f[f] + db, B.f[f] + sb, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->buf[0].ind + db, B.ind + sb, sizeof(int) * n, cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->buf[0].pid + db, B.pid + sb, sizeof(int) * n, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    CK(cudaMemcpyAsync(c->d_tstate + t, src->d_tstate + st_, sizeof(TubeState), cudaMemcpyDeviceToDevice, c->stream));
+  }
   for (int k = 0; k <= DS_NPHASE; k++) CK(cudaEventCreate(&c->ev[k]));
   CK(cudaStreamSynchronize(c->stream));
   c->finalized = true;
@@ -484,6 +510,7 @@ ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fi
     if (n > 0 && !fields[f]) return fail(c, DS_ERR_ARG, "required array is NULL");
   if (n > 0 && !ind) return fail(c, DS_ERR_ARG, "ind is NULL");
   if (!c->finalized) {
+    c->dev_src[tube] = std::make_pair((ds_ctx *)nullptr, 0);
     HostSpecies &H = c->host[tube][s];
     H.n = n;
     for (int f = 0; f < NF; f++) {
@@ -618,6 +645,7 @@ ds_status ds_create_batch(int ntubes, const ds_params *p, ds_ctx **out) {
   c->params.assign(p, p + ntubes);
   c->host.resize(ntubes);
   for (int t = 0; t < ntubes; t++) c->host[t].resize(1 + p[t].n_dust);
+  c->dev_src.assign(ntubes, std::make_pair((ds_ctx *)nullptr, 0));
   if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -647,6 +675,27 @@ ds_status ds_set_dust(ds_ctx *c, int tube, int species, int n, const double *x, 
   if (n > 0 && !t_stop) return fail(c, DS_ERR_ARG, "dust t_stop is required");
   const double *f[NF] = {x, y, z, vx, vy, vz, nullptr, nullptr, nullptr, rho, nullptr, nullptr, mas, h, t_stop};
   return set_species(c, tube, species, n, f, ind);
+}
+
+ds_status ds_copy_tube(ds_ctx *dst, int dst_tube, ds_ctx *src, int src_tube) {
+  if (!dst || !src || dst == src) return DS_ERR_ARG;
+  ds_ctx *c = dst;
+  if (dst->finalized) return fail(c, DS_ERR_STATE, "ds_copy_tube: destination already holds its state");
+  if (!src->finalized) return fail(c, DS_ERR_STATE, "ds_copy_tube: source has no resident state");
+  if (dst_tube < 0 || dst_tube >= dst->ntubes || src_tube < 0 || src_tube >= src->ntubes)
+    return fail(c, DS_ERR_ARG, "ds_copy_tube: bad tube index");
+  if (dst->device != src->device) return fail(c, DS_ERR_UNSUPPORTED, "ds_copy_tube: contexts on different devices");
+  const int nd = dst->params[dst_tube].n_dust;
+  if (nd != src->params[src_tube].n_dust) return fail(c, DS_ERR_ARG, "ds_copy_tube: species counts differ");
+  const TubeDesc &S = src->tdesc[src_tube];
+  for (int s = 0; s <= nd; s++) {
+    HostSpecies &H = dst->host[dst_tube][s];
+    H.n = S.seg_end[s] - S.seg_begin[s];
+    for (int f = 0; f < NF; f++) std::vector<double>().swap(H.f[f]);
+    std::vector<int>().swap(H.ind);
+  }
+  dst->dev_src[dst_tube] = std::make_pair(src, src_tube);
+  return DS_OK;
 }
 
 ds_status ds_upload_gas(ds_ctx *c, int n, const double *x, const double *y, const double *z, const double *vx,

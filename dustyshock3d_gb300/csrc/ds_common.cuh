@@ -278,7 +278,8 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 // stencil in the warp), and over each offset's cell in pieces of DS_PIECE
 // candidates (to the longest cell in the warp).  Each lane screens its own
 // candidates with a cheap FP32 test (`screen`) and appends survivors to its
-// column of the block's shared list (entry = offset code << 25 | slot).
+// column of the block's shared list (entry = offset code << 25 | slot - sb,
+// sb = the segment's first slot, so a segment may hold up to 2^25 particles).
 // When any lane's list could overflow, every lane runs `use(slot, offset
 // code)` over its entries, in visiting order, and the lists restart.  The
 // expensive pair work thus runs on dense lists with the warp converged,
@@ -291,7 +292,7 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 #define DS_SLOT_MASK ((1u << DS_OFS_SHIFT) - 1u)
 
 template <int CAP = DS_LIST_CAP, class Screen, class Use>
-__device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, bool act, int r, int kb,
+__device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, bool act, int r, int kb, int sb,
                                         const int *cell_start, uint32_t *lst, Screen screen, Use use) {
   const unsigned FULL = 0xffffffffu;
   const int w = 2 * r + 1;
@@ -304,7 +305,7 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
     for (int t = 0; t < nw; t++)
       if (t < n) {
         const uint32_t e = lst[t * DS_SWEEP_THREADS];
-        use((int)(e & DS_SLOT_MASK), (int)(e >> DS_OFS_SHIFT));
+        use(sb + (int)(e & DS_SLOT_MASK), (int)(e >> DS_OFS_SHIFT));
       }
     n = 0;
   };
@@ -336,7 +337,7 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
 #pragma unroll
       for (int t = 0; t < DS_PIECE; t++)
         if (pass[t]) {
-          lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t);
+          lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t - sb);
           n++;
         }
     }

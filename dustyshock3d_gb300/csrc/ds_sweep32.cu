@@ -47,9 +47,9 @@ __device__ __forceinline__ float dw_shape(float q) {
   return 0.0f;
 }
 
-template <bool HPP, int WHAT>
+template <bool HPP, int WHAT, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
-  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
+  __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
@@ -75,8 +75,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = hd <= T.r1_hmax ? 1 : T.stencil;
     Kahan sum;
-    ds_walk(
-        T, S, upd, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+    ds_walk<CAP>(
+        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
           const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
@@ -115,9 +115,9 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
   }
 }
 
-template <bool HPP>
+template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
-  __shared__ uint32_t lst[DS_LIST_CAP * DS_SWEEP_THREADS];
+  __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   const float c_pi = (float)(1.0 / 3.14159265);
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
@@ -140,8 +140,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
-    ds_walk(
-        T, S, act, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+    ds_walk<CAP>(
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
           const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
@@ -195,19 +195,30 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 
 }  // namespace
 
-void ds_launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
-  if (!a.nchunks) return;
+template <int CAP>
+static void launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
   if (what == 0) {
-    if (hpp) k_density32<true, 0><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_density32<false, 0><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    if (hpp) k_density32<true, 0, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_density32<false, 0, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
   } else {
-    if (hpp) k_density32<true, 1><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_density32<false, 1><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    if (hpp) k_density32<true, 1, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_density32<false, 1, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
   }
 }
 
-void ds_launch_force32(const SweepArgs &a, bool hpp, cudaStream_t s) {
+void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cudaStream_t s) {
   if (!a.nchunks) return;
-  if (hpp) k_force32<true><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-  else k_force32<false><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  if (depth >= 64) launch_density32<64>(a, hpp, what, s);
+  else launch_density32<32>(a, hpp, what, s);
+}
+
+void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) {
+  if (!a.nchunks) return;
+  if (depth >= 64) {
+    if (hpp) k_force32<true, 64><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_force32<false, 64><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  } else {
+    if (hpp) k_force32<true, 32><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    else k_force32<false, 32><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  }
 }

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
     int cur_o = -1;
     const double wn = ds_W_norm(hi);
     ds_walk<DS_LIST_CAP64>(
-        T, S, upd, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
           const float fx = pj.x + sx - pi.x, fy = pj.y + sy - pi.y, fz = pj.z + sz - pi.z;
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force64(SweepArgs a) {
     const float hif = (float)hi;
     const double dni = act ? a.dwn64[i] : 0.0;
     ds_walk<DS_LIST_CAP64>(
-        T, S, act, r, T.key_base[s], a.cell_start, lst + threadIdx.x,
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
         [&](int j, float sx, float sy, float sz) {
           const float4 pj = a.pos32[j];
           const float fx = pj.x + sx - pi.x, fy = pj.y + sy - pi.y, fz = pj.z + sz - pi.z;

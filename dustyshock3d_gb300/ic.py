@@ -207,3 +207,30 @@ def dusty_sod_tube(dx_left: float, Ly: float, Lz: float = None, eps: float = 1.0
     if fixed_tau:
         P.mode.cfl = False
     return P, [gas, dust]
+
+
+def uneven_tube(N_gas: float, rho_ratio: float, p_ratio: float, eps: float, t_s: float, t_end: float = 0.2,
+                n_across: int = 24, x_range=(-0.5, 0.5)) -> Tuple[Params, List[Species]]:
+    """A dusty Sod tube with about N_gas gas particles (and as many dust), left
+    state (rho 1, p 1), right state (1/rho_ratio, 1/p_ratio), n_across left
+    lattice sites across the periodic cross-section."""
+    L = x_range[1] - x_range[0]
+    dx_left = 0.5 * L * n_across * n_across * (1.0 + 1.0 / rho_ratio) / N_gas
+    return dusty_sod_tube(dx_left=dx_left, Ly=n_across * dx_left, eps=eps, t_s=t_s, rho_R=1.0 / rho_ratio,
+                          p_R=1.0 / p_ratio, t_end=t_end, x_range=x_range)
+
+
+def draw_tube_params(rng, n_range=(2.0e4, 1.0e6)):
+    """One tube of the uneven-batch distributions: particle count per phase
+    log-uniform in n_range, density ratio U[4, 16], pressure ratio U[5, 20],
+    eps log-U[0.01, 10], t_s log-U[1e-4, 1e-1]."""
+    lo, hi = np.log(n_range[0]), np.log(n_range[1])
+    return dict(N_gas=float(np.exp(rng.uniform(lo, hi))), rho_ratio=float(rng.uniform(4.0, 16.0)),
+                p_ratio=float(rng.uniform(5.0, 20.0)), eps=float(np.exp(rng.uniform(np.log(0.01), np.log(10.0)))),
+                t_s=float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-1)))))
+
+
+def batch_tubes(seed: int = 2026, n_tubes: int = 64, n_range=(2.0e4, 1.0e6), t_end: float = 0.2):
+    """The seeded batch of uneven tubes: a list of (params, species)."""
+    rng = np.random.default_rng(seed)
+    return [uneven_tube(t_end=t_end, **draw_tube_params(rng, n_range)) for _ in range(n_tubes)]

@@ -67,6 +67,11 @@ class Solver:
         _lib.check(self.L, self.ctx, st, f"set species {s} of tube {tube}")
         self.n[tube][s] = n
 
+    def copy_tube_from(self, tube: int, src: "Solver", src_tube: int):
+        """Carry a running tube of ``src`` into ``tube`` (device to device, at the first step)."""
+        _lib.check(self.L, self.ctx, self.L.ds_copy_tube(self.ctx, tube, src.ctx, src_tube), "ds_copy_tube")
+        self.n[tube] = list(src.n[src_tube])
+
     def set_tube(self, tube: int, species: Sequence[Species]):
         for s, sp in enumerate(species):
             self.set_species(tube, s, sp.copy().fill_missing())

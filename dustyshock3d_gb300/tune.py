@@ -1,0 +1,80 @@
+"""Autotuner for the FP32 neighbour sweeps of a batch of tubes.
+
+Knobs (all results stay within the FP32 path's tolerance; none changes the
+physics):
+  * cell size and stencil: cells of width ~h_max searched 2 cells on each side
+    (a particle whose cut-off fits walks only the 27 inner cells), or cells of
+    width ~2 h_max searched 1 cell on each side; plus the cell-width margin;
+  * list depth: candidate-list entries per thread (32 or 64), i.e. how many
+    screened neighbours a thread stages before the pair work runs.
+
+The tuner times a few steps of each candidate on a sample of the batch (the
+first ``sample`` tubes) with CUDA events and returns the fastest.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Sequence, Tuple
+
+from .params import Params
+from .solver import Solver
+from .species import Species
+
+# (stencil, cell width / h_max, list depth)
+CANDIDATES = [
+    (2, 1.001, 32),
+    (2, 1.001, 64),
+    (2, 1.10, 32),
+    (1, 2.002, 32),
+]
+
+
+@dataclasses.dataclass
+class Choice:
+    stencil: int
+    cell_factor: float
+    list_depth: int
+    ms_per_step: float
+
+
+def apply(P: Params, stencil: int, cell_factor: float, list_depth: int) -> Params:
+    Q = P.copy()
+    Q.stencil = stencil
+    Q.cell_w = cell_factor * Q.h  # Q.h is the tube's largest smoothing length
+    Q.list_depth = list_depth
+    return Q
+
+
+def _fits(P: Params) -> bool:
+    """Periodic axes need 2*stencil+1 cells."""
+    w = P.cell_width()
+    need = 2 * P.stencil + 1
+    if P.mode.periodic_y and int((P.Y_max - P.Y_min) / w) < need:
+        return False
+    if P.mode.periodic_z and int((P.Z_max - P.Z_min) / w) < need:
+        return False
+    return True
+
+
+def tune(tubes: Sequence[Tuple[Params, List[Species]]], sample: int = 8, warmup: int = 2, steps: int = 3,
+         precision: str = "fp32", candidates=CANDIDATES) -> Tuple[Choice, list]:
+    sub = list(tubes[:sample])
+    log = []
+    best = None
+    for stencil, factor, depth in candidates:
+        ps = [apply(P, stencil, factor, depth) for P, _ in sub]
+        for q in ps:
+            q.precision = precision
+        if not all(_fits(q) for q in ps):
+            log.append((stencil, factor, depth, None))
+            continue
+        with Solver(ps) as S:
+            for t, (_, sp) in enumerate(sub):
+                S.set_tube(t, sp)
+            S.step(warmup)
+            ms, _ = S.step_timed(steps)
+        ms /= steps
+        log.append((stencil, factor, depth, ms))
+        if best is None or ms < best.ms_per_step:
+            best = Choice(stencil, factor, depth, ms)
+    return best, log

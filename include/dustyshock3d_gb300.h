@@ -91,6 +91,9 @@ typedef struct ds_params {
   double idic_w;             /* IDIC cell width; 0 -> Coeff_h_dust_cell*h (kernel.cu:1577) */
   double cfl;                /* CFL number (DS_MODE_CFL)                          */
   double t_empty;            /* mean t_stop of a cell without dust (kernel.cu:2160) */
+  int list_depth;             /* FP32 sweeps: candidate-list entries per thread, 32 or 64
+                                (0 -> 32); an autotuner choice                         */
+  int reserved1;
   double mass_ratio[DS_MAX_DUST];   /* mas_gas_dust_k (kernel.cu:1499-1502)       */
   double R_dust[DS_MAX_DUST];       /* R_dust_k for t_stop = R/(c_s rho) (IDIC.h:86) */
   double t_stop_const[DS_MAX_DUST]; /* DS_MODE_TSTOP_CONST                        */
@@ -125,6 +128,14 @@ ds_status ds_set_dust(ds_ctx *c, int tube, int species, int n, const double *x, 
                       const double *z, const double *vx, const double *vy, const double *vz,
                       const double *rho, const double *mas, const double *t_stop, const double *h,
                       const int *ind);
+
+/* Carries tube src_tube of src's resident state (particles in their current
+ * order, simulation time and step count) into tube dst_tube of dst, which must
+ * not have stepped yet; the copy is device to device, made when dst is first
+ * stepped, so src must stay alive until then.  Particle counts per species are
+ * src's; parameters are dst's.  A batch is rebuilt this way when tubes join or
+ * leave it (continuous batching), without the state leaving the GPU. */
+ds_status ds_copy_tube(ds_ctx *dst, int dst_tube, ds_ctx *src, int src_tube);
 
 /* Single-tube names the reference's host driver binds (tube 0). */
 ds_status ds_upload_gas(ds_ctx *c, int n, const double *x, const double *y, const double *z,

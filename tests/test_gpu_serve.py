@@ -1,0 +1,51 @@
+"""Continuous batching: requests that join and leave a running batch get the
+same result as when solved alone (bit for bit: a tube's arithmetic does not
+depend on the other tubes of its batch)."""
+import numpy as np
+import pytest
+
+from dustyshock3d_gb300 import ic
+from dustyshock3d_gb300.serve import Request, Server, memory_estimate, run_alone
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    shapes = [dict(eps=1.0, t_s=1e-3), dict(eps=0.1, t_s=1e-2, rho_R=0.25, p_R=0.2),
+              dict(eps=3.0, t_s=3e-4), dict(eps=0.5, t_s=5e-2, rho_R=0.1, p_R=0.125)]
+    out = []
+    for i, kw in enumerate(shapes):
+        P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25), **kw)
+        out.append(Request(i, 0.05 * i, P, sp, t_end=0.012 + 0.006 * i))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_mix_equals_alone(precision):
+    reqs = _requests()
+    server = Server(budget_bytes=150e9, epoch_steps=2, precision=precision)
+    results = server.run(reqs)
+    assert [r.rid for r in results] == [0, 1, 2, 3]
+    assert server.rebuilds >= 2, "requests should have joined a running batch"
+    for req, res in zip(reqs, results):
+        alone = run_alone(req, precision)
+        for s in range(2):
+            for f in ("x", "y", "z", "vx", "vy", "vz", "rho"):
+                a, b = getattr(res.species[s], f), getattr(alone[s], f)
+                assert np.array_equal(a, b), f"request {req.rid} species {s} {f}"
+        assert res.time_to_solution >= 0
+
+
+def test_budget_admits_one_at_a_time():
+    reqs = _requests()[:3]
+    one = max(memory_estimate(r.params, r.species) for r in reqs)
+    server = Server(budget_bytes=1.2 * one, epoch_steps=4, precision="fp32")
+    results = server.run(reqs)
+    assert len(results) == 3
+    # never two tubes at once: each admitted after the previous finished
+    order = sorted(results, key=lambda r: r.admitted)
+    for a, b in zip(order, order[1:]):
+        assert b.admitted >= a.finished - 1e-9
+    for req, res in zip(reqs, results):
+        alone = run_alone(req, "fp32")
+        assert np.array_equal(res.species[0].rho, alone[0].rho)

@@ -1,0 +1,40 @@
+"""Host-side logic of the server and the batch generator (no GPU)."""
+import numpy as np
+
+from dustyshock3d_gb300 import ic
+from dustyshock3d_gb300.serve import grid_sizes, memory_estimate, poisson_requests
+from oracle.oracle import OracleState
+
+
+def test_grid_sizes_match_oracle():
+    for P, sp in [ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25)),
+                  ic.dusty_sod_tube(dx_left=1 / 200, Ly=0.1)]:
+        info = OracleState(P, sp).grid_info()
+        nc, ni = grid_sizes(P)
+        assert nc == info[3] and ni == info[7]
+
+
+def test_memory_estimate_scales_with_particles():
+    P1, s1 = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25))
+    P2, s2 = ic.dusty_sod_tube(dx_left=1 / 128, Ly=0.25, x_range=(-0.25, 0.25))
+    assert memory_estimate(P2, s2) > 4 * memory_estimate(P1, s1)
+
+
+def test_poisson_arrivals_seeded():
+    mk = lambda rng: ic.dusty_sod_tube(dx_left=1 / 32, Ly=0.25, x_range=(-0.25, 0.25))  # noqa: E731
+    a = poisson_requests(5.0, 6, 7, mk)
+    b = poisson_requests(5.0, 6, 7, mk)
+    assert [r.arrival for r in a] == [r.arrival for r in b]
+    assert all(0.05 <= r.t_end <= 0.2 for r in a)
+    assert np.all(np.diff([r.arrival for r in a]) > 0)
+
+
+def test_batch_distributions():
+    rng = np.random.default_rng(1)
+    d = [ic.draw_tube_params(rng) for _ in range(2000)]
+    n = np.array([x["N_gas"] for x in d])
+    assert n.min() >= 2e4 and n.max() <= 1e6
+    assert 4 <= min(x["rho_ratio"] for x in d) and max(x["rho_ratio"] for x in d) <= 16
+    assert 5 <= min(x["p_ratio"] for x in d) and max(x["p_ratio"] for x in d) <= 20
+    e = np.log10([x["eps"] for x in d])
+    assert -2 <= e.min() and e.max() <= 1 and abs(np.median(e) + 0.5) < 0.1
