@@ -231,21 +231,52 @@ __device__ __forceinline__ int ds_stencil_cell(const TubeDesc &T, const Stencil 
   return cx + cy * T.sy + cz * T.sz;
 }
 
-// FP32 shift that brings a neighbour cell's FP32 coordinates into ours:
-// whole cell widths when coordinates are cell-relative (this also applies the
-// periodic image), the image shift when they are tube-relative.  wf holds the
-// cell widths in FP32 so the shift costs no FP64 work.
-__device__ __forceinline__ void ds_pre_shift(const TubeDesc &T, const float3 &wf, int k, int l, int g, double shy,
-                                             double shz, float &sx, float &sy, float &sz) {
+// FP32 cell widths and periodic lengths of a tube, converted once per thread
+// so that the per-candidate shifts below cost no FP64 work.
+struct Shift32 {
+  float wx, wy, wz, Ly, Lz;
+};
+
+__device__ __forceinline__ Shift32 ds_shift32_init(const TubeDesc &T) {
+  return Shift32{(float)T.wx, (float)T.wy, (float)T.wz, (float)T.Ly, (float)T.Lz};
+}
+
+// FP32 shift that brings the FP32 coordinates of the neighbour cell at
+// offsets (k, l, g) into ours: whole cell widths when coordinates are
+// cell-relative (this also applies the periodic image), the periodic image
+// shift when they are tube-relative on a proper grid, none on the reference
+// grid.  The image shift is +-(float)L, which equals (float)(+-L), the FP64
+// image shift rounded once.
+__device__ __forceinline__ void ds_shift32(const TubeDesc &T, const Stencil &S, const Shift32 &f, int k, int l,
+                                           int g, float &sx, float &sy, float &sz) {
   if (T.cellrel) {
-    sx = (float)k * wf.x;
-    sy = (float)l * wf.y;
-    sz = (float)g * wf.z;
-  } else {
-    sx = 0.0f;
-    sy = (float)shy;
-    sz = (float)shz;
+    sx = (float)k * f.wx;
+    sy = (float)l * f.wy;
+    sz = (float)g * f.wz;
+    return;
   }
+  sx = sy = sz = 0.0f;
+  if (!(T.mode & M_GRID_PROPER)) return;
+  if (T.mode & M_PER_Y) {
+    const int cy = S.iy + l;
+    sy = cy < 0 ? -f.Ly : (cy >= T.ny ? f.Ly : 0.0f);
+  }
+  if (T.mode & M_PER_Z) {
+    const int cz = S.iz + g;
+    sz = cz < 0 ? -f.Lz : (cz >= T.nz ? f.Lz : 0.0f);
+  }
+}
+
+// Shift of a list entry's cell minus the particle's own FP32 coordinates, as
+// ds_walk hands it to the screen (the same two roundings, so the pair work
+// sees the offsets the screen saw).
+__device__ __forceinline__ void ds_rel_shift32(const TubeDesc &T, const Stencil &S, const Shift32 &f,
+                                               const float4 &pi, int o5, float &ox, float &oy, float &oz) {
+  const int k = o5 / 25 - 2, l = (o5 / 5) % 5 - 2, g = o5 % 5 - 2;
+  ds_shift32(T, S, f, k, l, g, ox, oy, oz);
+  ox -= pi.x;
+  oy -= pi.y;
+  oz -= pi.z;
 }
 
 // Image shifts of the neighbour cell at offsets (l, g) from the own cell.
@@ -277,12 +308,14 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 // All 32 lanes run the same loops: over the stencil offsets (to the largest
 // stencil in the warp), and over each offset's cell in pieces of DS_PIECE
 // candidates (to the longest cell in the warp).  Each lane screens its own
-// candidates with a cheap FP32 test (`screen`) and appends survivors to its
-// column of the block's shared list (entry = offset code << 25 | slot - sb,
-// sb = the segment's first slot, so a segment may hold up to 2^25 particles).
-// When any lane's list could overflow, every lane runs `use(slot, offset
-// code)` over its entries, in visiting order, and the lists restart.  The
-// expensive pair work thus runs on dense lists with the warp converged,
+// candidates with a cheap FP32 test (`screen(slot, ox, oy, oz)`, where
+// (ox, oy, oz) = the cell's FP32 shift minus the particle's own FP32
+// coordinates, so a candidate's offset is pos32 + o) and appends survivors to
+// its column of the block's shared list (entry = offset code << 25 | slot -
+// sb, sb = the segment's first slot, so a segment may hold up to 2^25
+// particles).  When any lane's list could overflow, every lane runs `use(slot,
+// offset code)` over its entries, in visiting order, and the lists restart.
+// The expensive pair work thus runs on dense lists with the warp converged,
 // instead of a warp idling while one lane meets a neighbour.  Lanes without a
 // particle (act false) take part with empty stencils.
 #define DS_SWEEP_THREADS 128
@@ -293,12 +326,13 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 
 template <int CAP = DS_LIST_CAP, class Screen, class Use>
 __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, bool act, int r, int kb, int sb,
-                                        const int *cell_start, uint32_t *lst, Screen screen, Use use) {
+                                        const int *cell_start, const float4 &pi, uint32_t *lst, Screen screen,
+                                        Use use) {
   const unsigned FULL = 0xffffffffu;
   const int w = 2 * r + 1;
   const int nofs = act ? w * w * w : 0;
   const int nofs_w = __reduce_max_sync(FULL, nofs);
-  const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
+  const Shift32 f32 = ds_shift32_init(T);
   int n = 0;
   auto flush = [&]() {
     const int nw = __reduce_max_sync(FULL, n);
@@ -321,7 +355,10 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
         j0 = cell_start[kb + cell];
         j1 = cell_start[kb + cell + 1];
       }
-      ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+      ds_shift32(T, S, f32, k, l, g, sx, sy, sz);
+      sx -= pi.x;
+      sy -= pi.y;
+      sz -= pi.z;
       code = (uint32_t)((k + 2) * 25 + (l + 2) * 5 + (g + 2)) << DS_OFS_SHIFT;
     }
     const int len_w = __reduce_max_sync(FULL, j1 - j0);
@@ -332,7 +369,7 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
 #pragma unroll
       for (int t = 0; t < DS_PIECE; t++) {
         const int j = j0 + p0 + t;
-        pass[t] = (p0 + t < len_w) && (j < j1) && screen(j, sx, sy, sz);
+        pass[t] = (j < j1) && screen(j, sx, sy, sz);  // j1 - j0 <= len_w
       }
 #pragma unroll
       for (int t = 0; t < DS_PIECE; t++)

@@ -70,27 +70,23 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
     const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
     const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
-    const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
+    const Shift32 f32 = ds_shift32_init(T);
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = hd <= T.r1_hmax ? 1 : T.stencil;
     Kahan sum;
     ds_walk<CAP>(
-        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
-        [&](int j, float sx, float sy, float sz) {
+        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
+        [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
           return dx * dx + dy * dy + dz * dz < cut2;
         },
         [&](int j, int o5) {
-          int k, l, g;
-          ds_decode_ofs(o5, k, l, g);
-          double shy, shz;
-          ds_wrap_shift(T, S, l, g, shy, shz);
-          float sx, sy, sz;
-          ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+          float ox, oy, oz;
+          ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
           sum.add(a.vm32[j].w * w_shape(sqrtf(dx * dx + dy * dy + dz * dz) * inv_h));
         });
     if (!valid) continue;
@@ -135,29 +131,25 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
     const float mi = vmi.w, rhoi = hyi.z, pti = hyi.y, csi = hyi.x;
     const float mpi = act ? (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i])) : 0.0f;
     const float alpha = (float)T.alpha, beta = (float)T.beta, eps = (float)T.eps;
-    const float3 wf = make_float3((float)T.wx, (float)T.wy, (float)T.wz);
+    const Shift32 f32 = ds_shift32_init(T);
     Kahan Ax, Ay, Az, et;
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
     ds_walk<CAP>(
-        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
-        [&](int j, float sx, float sy, float sz) {
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
+        [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
           const float r2 = dx * dx + dy * dy + dz * dz;
           const float hc = HPP ? fmaxf(hi, pj.w) : hi;
           return (r2 < 4.0f * hc * hc) && (r2 > 0.0f);
         },
         [&](int j, int o5) {
-          int k, l, g;
-          ds_decode_ofs(o5, k, l, g);
-          double shy, shz;
-          ds_wrap_shift(T, S, l, g, shy, shz);
-          float sx, sy, sz;
-          ds_pre_shift(T, wf, k, l, g, shy, shz, sx, sy, sz);
+          float ox, oy, oz;
+          ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + sx - pi.x, dy = pj.y + sy - pi.y, dz = pj.z + sz - pi.z;
+          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
           const float r2 = dx * dx + dy * dy + dz * dz;
           const float inv_d = rsqrtf(r2);
           const float dist = r2 * inv_d;

@@ -71,10 +71,10 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
     int cur_o = -1;
     const double wn = ds_W_norm(hi);
     ds_walk<DS_LIST_CAP64>(
-        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
-        [&](int j, float sx, float sy, float sz) {
+        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
+        [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
-          const float fx = pj.x + sx - pi.x, fy = pj.y + sy - pi.y, fz = pj.z + sz - pi.z;
+          const float fx = pj.x + ox, fy = pj.y + oy, fz = pj.z + oz;
           return fx * fx + fy * fy + fz * fz <= cut2;  // beyond: W = 0
         },
         [&](int j, int o5) {
@@ -148,10 +148,10 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force64(SweepArgs a) {
     const float hif = (float)hi;
     const double dni = act ? a.dwn64[i] : 0.0;
     ds_walk<DS_LIST_CAP64>(
-        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, lst + threadIdx.x,
-        [&](int j, float sx, float sy, float sz) {
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
+        [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
-          const float fx = pj.x + sx - pi.x, fy = pj.y + sy - pi.y, fz = pj.z + sz - pi.z;
+          const float fx = pj.x + ox, fy = pj.y + oy, fz = pj.z + oz;
           const float hcf = HPP ? fmaxf(hif, pj.w) : hif;
           return fx * fx + fy * fy + fz * fz <= pre_cut2(2.0f * hcf, T.pre_abs);
         },
