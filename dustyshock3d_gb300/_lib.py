@@ -33,7 +33,7 @@ class DsParams(ctypes.Structure):
         ("Gam_g", ctypes.c_double), ("Speed_of_sound_gas", ctypes.c_double),
         ("n_dust", ctypes.c_int), ("mode", ctypes.c_int), ("precision", ctypes.c_int), ("stencil", ctypes.c_int),
         ("cell_w", ctypes.c_double), ("idic_w", ctypes.c_double), ("cfl", ctypes.c_double),
-        ("t_empty", ctypes.c_double), ("list_depth", ctypes.c_int), ("reserved1", ctypes.c_int),
+        ("t_empty", ctypes.c_double), ("list_depth", ctypes.c_int), ("force_list", ctypes.c_int),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
         ("t_stop_const", ctypes.c_double * MAX_DUST), ("eps_empty", ctypes.c_double * MAX_DUST),
     ]
@@ -120,6 +120,7 @@ def params_to_c(P: Params) -> DsParams:
     c.precision = 1 if str(P.precision).lower() in ("fp32", "1") else 0
     c.stencil = int(getattr(P, "stencil", 1) or 1)
     c.list_depth = int(getattr(P, "list_depth", 0) or 0)
+    c.force_list = int(getattr(P, "force_list", 0) or 0)
     for k in range(MAX_DUST):
         c.mass_ratio[k] = float(P.mass_ratio[k]) if k < len(P.mass_ratio) else 0.0
         c.R_dust[k] = float(P.R_dust[k]) if k < len(P.R_dust) else 0.0

@@ -77,6 +77,10 @@ struct ds_ctx {
   bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
   double *cs64 = nullptr, *pt64 = nullptr, *dwn64 = nullptr, *edot = nullptr;
+  uint32_t *nbl = nullptr;  // FP32 force neighbour lists, nbl_cap entries per gas slot of each chunk
+  int *nbl_cnt = nullptr;
+  unsigned char *nbl_walk = nullptr;
+  int nbl_cap = 0;
   uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
   uint32_t *ikin = nullptr, *ivin = nullptr, *ikalt = nullptr, *ivalt = nullptr;
   uint32_t *rs_scratch = nullptr;
@@ -94,6 +98,8 @@ struct ds_ctx {
   cudaEvent_t ev[DS_NPHASE + 1] = {};
   std::vector<cudaEvent_t> tev;
 };
+
+static_assert(DS_CHUNK == DS_SWEEP_THREADS, "one sweep thread per particle of a chunk");
 
 namespace {
 
@@ -218,6 +224,7 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
   if (P.stencil != 0 && P.stencil != 1 && P.stencil != 2) return fail(c, DS_ERR_ARG, "stencil must be 1 or 2");
   if (P.list_depth != 0 && P.list_depth != 32 && P.list_depth != 64)
     return fail(c, DS_ERR_ARG, "list_depth must be 0, 32 or 64");
+  if (P.force_list < -1 || P.force_list > 4096) return fail(c, DS_ERR_ARG, "force_list must be -1, 0 or 1..4096");
   if (P.stencil == 2 && !(P.mode & DS_MODE_GRID_PROPER))
     return fail(c, DS_ERR_UNSUPPORTED, "stencil 2 needs the proper cell grid (DS_MODE_GRID_PROPER)");
   const int need = 2 * T.stencil + 1;  // a periodic axis must not alias its own stencil
@@ -259,6 +266,10 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.gas_ind_pid = c->ind_of_pid;
   a.tstate_rw = c->d_tstate;
   a.flags = c->d_flags;
+  a.nbl = nullptr;
+  a.nbl_cnt = nullptr;
+  a.nbl_walk = nullptr;
+  a.nbl_cap = 0;
   return a;
 }
 
@@ -295,6 +306,12 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
   const bool fp32 = c->any_fp32;
   SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
   SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
+  if (c->nbl) {
+    ag.nbl = c->nbl;
+    ag.nbl_cnt = c->nbl_cnt;
+    ag.nbl_walk = c->nbl_walk;
+    ag.nbl_cap = c->nbl_cap;
+  }
   const int depth = c->params[0].list_depth;
   if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
@@ -405,6 +422,13 @@ ds_status finalize(ds_ctx *c) {
   DA(c->krad, (size_t)nkeys);
   CK(cudaMemsetAsync(c->krad, 1, (size_t)nkeys, c->stream));
   DA(c->stage, N);
+  if (c->any_fp32 && c->params[0].force_list != -1 && !c->ch_gas.empty()) {
+    // the force sweep's neighbours, recorded by the gas density sweep
+    c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : 256;
+    DA(c->nbl, c->ch_gas.size() * (size_t)c->nbl_cap * DS_CHUNK);
+    DA(c->nbl_cnt, N);
+    DA(c->nbl_walk, c->ch_gas.size());
+  }
   DA(c->d_cons, 8);
   DA(c->d_flags, 1);
   DA(c->ca.cnt, nikeys);
@@ -779,7 +803,7 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
   *count = 13 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
-           (c->any_stencil2 ? 2 : 0);
+           (c->any_stencil2 ? 2 : 0) + (c->nbl ? 1 : 0);
   return DS_OK;
 }
 

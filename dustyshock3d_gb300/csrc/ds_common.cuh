@@ -409,4 +409,10 @@ struct SweepArgs {
   const int *gas_ind_pid;      // gas Ind by pid (index-coupled dust rho zeroing)
   TubeState *tstate_rw;
   int *flags;
+  // FP32 force neighbour lists (recorded by the gas density sweep): entry e of
+  // the particle in lane t of gas chunk c at nbl[(c * nbl_cap + e) * 128 + t]
+  uint32_t *nbl;               // nullptr: the force sweep walks the cells
+  int *nbl_cnt;                // entries per slot
+  unsigned char *nbl_walk;     // per gas chunk: 1 when a particle overflowed (that chunk walks)
+  int nbl_cap;
 };

@@ -47,8 +47,22 @@ __device__ __forceinline__ float dw_shape(float q) {
   return 0.0f;
 }
 
-template <bool HPP, int WHAT, int CAP>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
+// Squared distance with explicit roundings (no contraction chosen by the
+// compiler), so the density sweep's screen, the force sweep's screen and the
+// pair work all see the same value for the same pair.
+__device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// LIST: the gas density sweep also records the force sweep's neighbours.  It
+// then walks the force sweep's stencil and screens with its cut-off
+// 2 max(h_i, h_j) (a superset of its own 2 h_i: the density adds only pairs
+// within 2 h_i, so its sum is unchanged), and writes each pair with r > 0 --
+// exactly the pairs the force sweep's own walk would accept, in its visiting
+// order.  A chunk with a particle beyond nbl_cap entries is flagged; the force
+// sweep walks that chunk.
+template <bool HPP, int WHAT, int CAP, bool LIST>
+__global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 6 : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
@@ -73,22 +87,39 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
     const Shift32 f32 = ds_shift32_init(T);
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
-    const int r = hd <= T.r1_hmax ? 1 : T.stencil;
+    const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[a.skey[i]]) : (hd <= T.r1_hmax ? 1 : T.stencil);
+    const int sb = T.seg_begin[s];
+    uint32_t *nl = LIST ? a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x : nullptr;
+    int cnt = 0;
     Kahan sum;
     ds_walk<CAP>(
-        T, S, upd, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
+        T, S, upd, r, T.key_base[s], sb, a.cell_start, pi, lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
-          return dx * dx + dy * dy + dz * dz < cut2;
+          const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
+          if (LIST) {
+            const float hc = HPP ? fmaxf(hf, pj.w) : hf;
+            return r2 < 4.0f * hc * hc;
+          }
+          return r2 < cut2;
         },
         [&](int j, int o5) {
           float ox, oy, oz;
           ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
           const float4 pj = a.pos32[j];
-          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
-          sum.add(a.vm32[j].w * w_shape(sqrtf(dx * dx + dy * dy + dz * dz) * inv_h));
+          const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
+          if (!LIST || r2 < cut2) sum.add(a.vm32[j].w * w_shape(sqrtf(r2) * inv_h));
+          if (LIST && r2 > 0.0f) {
+            if (cnt < a.nbl_cap)
+              nl[(size_t)cnt * DS_SWEEP_THREADS] = ((uint32_t)o5 << DS_OFS_SHIFT) | (uint32_t)(j - sb);
+            cnt++;
+          }
         });
+    if (LIST) {
+      const int over = __syncthreads_or(cnt > a.nbl_cap);
+      if (threadIdx.x == 0) a.nbl_walk[c] = (unsigned char)(over != 0);
+      if (i < ch.end) a.nbl_cnt[i] = cnt;
+    }
     if (!valid) continue;
     if (upd) rho = rho + (((double)1 / (DS_PI_REF)) / (hd * hd * hd)) * sum.value();
     if (zero || upd) a.st.rho[i] = rho;
@@ -111,77 +142,133 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32(SweepArgs a) {
   }
 }
 
+// Per-particle state and pair work of the force sweep (ForceKernel_IDIC,
+// IDIC.h:198-260, in FP32 with Kahan sums).
+template <bool HPP>
+struct ForceSum {
+  float4 pi, vmi;
+  float hi, inv_hi, ni, mi, rhoi, pti, csi, mpi, alpha, beta, eps;
+  Shift32 f32;
+  Kahan Ax, Ay, Az, et;
+
+  __device__ __forceinline__ ForceSum(const SweepArgs &a, const TubeDesc &T, int i, bool act) {
+    pi = act ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 1.f);
+    vmi = act ? a.vm32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 hyi = act ? a.hyd32[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    hi = HPP ? pi.w : (float)T.h;
+    inv_hi = 1.0f / hi;
+    ni = (float)(1.0 / 3.14159265) * inv_hi * inv_hi * inv_hi * inv_hi;
+    mi = vmi.w;
+    rhoi = hyi.z;
+    pti = hyi.y;
+    csi = hyi.x;
+    mpi = act ? (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i])) : 0.0f;
+    alpha = (float)T.alpha;
+    beta = (float)T.beta;
+    eps = (float)T.eps;
+    f32 = ds_shift32_init(T);
+  }
+
+  // the force sweep's screen: 0 < r < 2 max(h_i, h_j)
+  __device__ __forceinline__ bool screen(const float4 &pj, float ox, float oy, float oz) const {
+    const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
+    const float hc = HPP ? fmaxf(hi, pj.w) : hi;
+    return (r2 < 4.0f * hc * hc) && (r2 > 0.0f);
+  }
+
+  __device__ __forceinline__ void pair(const SweepArgs &a, const TubeDesc &T, const Stencil &S, int j, int o5) {
+    float ox, oy, oz;
+    ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
+    const float4 pj = a.pos32[j];
+    const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
+    const float r2 = r2_of(dx, dy, dz);
+    const float inv_d = rsqrtf(r2);
+    const float dist = r2 * inv_d;
+    const float hj = HPP ? pj.w : hi;
+    const float4 vmj = a.vm32[j];
+    const float4 hyj = a.hyd32[j];
+    const float hh = HPP ? 0.5f * (hi + hj) : hi;
+    const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
+    float F = 0.0f;
+    if (nu < 0.0f) {
+      const float Cnu = 0.5f * (csi + hyj.x);
+      const float mu = hh * nu / (r2 + eps * hh * hh);
+      F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
+    }
+    float dWr = ni * dw_shape(dist * inv_hi);
+    if (HPP) {
+      const float inv_hj = 1.0f / hj;
+      const float nj = (float)(1.0 / 3.14159265) * inv_hj * inv_hj * inv_hj * inv_hj;
+      dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
+    }
+    const float gd = dWr * inv_d;
+    et.add((mpi + mi * F * 0.5f) * nu * gd);
+    const float A = vmj.w * (pti + hyj.y + F) * gd;
+    Ax.add(dx * A);
+    Ay.add(dy * A);
+    Az.add(dz * A);
+  }
+
+  __device__ __forceinline__ void store(const SweepArgs &a, int i) const {
+    a.st.ax[i] = Ax.value();
+    a.st.ay[i] = Ay.value();
+    a.st.az[i] = Az.value();
+    a.edot[i] = et.value();
+  }
+};
+
+// Force sweep by walking the stencil.  With recorded lists it runs only the
+// chunks flagged as overflowed.
 template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
-  const float c_pi = (float)(1.0 / 3.14159265);
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    if (a.nbl && !a.nbl_walk[c]) continue;
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
     const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int s = ch.species;
     const double xi = act ? a.st.x[i] : 0.0, yi = act ? a.st.y[i] : 0.0, zi = act ? a.st.z[i] : 0.0;
-    const float4 pi = act ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 1.f);
-    const float4 vmi = act ? a.vm32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 hyi = act ? a.hyd32[i] : make_float4(0.f, 0.f, 1.f, 0.f);
-    const float hi = HPP ? pi.w : (float)T.h;
-    const float inv_hi = 1.0f / hi;
-    const float ni = c_pi * inv_hi * inv_hi * inv_hi * inv_hi;
-    const float mi = vmi.w, rhoi = hyi.z, pti = hyi.y, csi = hyi.x;
-    const float mpi = act ? (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i])) : 0.0f;
-    const float alpha = (float)T.alpha, beta = (float)T.beta, eps = (float)T.eps;
-    const Shift32 f32 = ds_shift32_init(T);
-    Kahan Ax, Ay, Az, et;
+    ForceSum<HPP> F(a, T, i, act);
     Stencil S;
     ds_stencil_init(T, xi, yi, zi, S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
     ds_walk<CAP>(
-        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, pi, lst + threadIdx.x,
-        [&](int j, float ox, float oy, float oz) {
-          const float4 pj = a.pos32[j];
-          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const float hc = HPP ? fmaxf(hi, pj.w) : hi;
-          return (r2 < 4.0f * hc * hc) && (r2 > 0.0f);
-        },
-        [&](int j, int o5) {
-          float ox, oy, oz;
-          ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
-          const float4 pj = a.pos32[j];
-          const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const float inv_d = rsqrtf(r2);
-          const float dist = r2 * inv_d;
-          const float hj = HPP ? pj.w : hi;
-          const float4 vmj = a.vm32[j];
-          const float4 hyj = a.hyd32[j];
-          const float hh = HPP ? 0.5f * (hi + hj) : hi;
-          const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
-          float F = 0.0f;
-          if (nu < 0.0f) {
-            const float Cnu = 0.5f * (csi + hyj.x);
-            const float mu = hh * nu / (r2 + eps * hh * hh);
-            F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
-          }
-          float dWr = ni * dw_shape(dist * inv_hi);
-          if (HPP) {
-            const float inv_hj = 1.0f / hj;
-            const float nj = c_pi * inv_hj * inv_hj * inv_hj * inv_hj;
-            dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
-          }
-          const float gd = dWr * inv_d;
-          et.add((mpi + mi * F * 0.5f) * nu * gd);
-          const float A = vmj.w * (pti + hyj.y + F) * gd;
-          Ax.add(dx * A);
-          Ay.add(dy * A);
-          Az.add(dz * A);
-        });
-    if (!act) continue;
-    a.st.ax[i] = Ax.value();
-    a.st.ay[i] = Ay.value();
-    a.st.az[i] = Az.value();
-    a.edot[i] = et.value();
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, lst + threadIdx.x,
+        [&](int j, float ox, float oy, float oz) { return F.screen(a.pos32[j], ox, oy, oz); },
+        [&](int j, int o5) { F.pair(a, T, S, j, o5); });
+    if (act) F.store(a, i);
+  }
+}
+
+// Force sweep over the recorded lists: no cell walk, no screening; entries in
+// the walk's order, so the sums equal the walk's.
+template <bool HPP>
+__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
+  const unsigned FULL = 0xffffffffu;
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    if (a.nbl_walk[c]) continue;
+    const Chunk ch = a.chunks[c];
+    const int i = ch.begin + threadIdx.x;
+    const TubeDesc &T = a.tubes[ch.tube];
+    const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
+    const int sb = T.seg_begin[ch.species];
+    ForceSum<HPP> F(a, T, i, act);
+    Stencil S;
+    ds_stencil_init(T, act ? a.st.x[i] : 0.0, act ? a.st.y[i] : 0.0, act ? a.st.z[i] : 0.0, S);
+    const int cnt = act ? a.nbl_cnt[i] : 0;
+    const int cnt_w = __reduce_max_sync(FULL, cnt);
+    const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
+    for (int e = 0; e < cnt_w; e += DS_PIECE) {
+      uint32_t ent[DS_PIECE];
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++) ent[t] = e + t < cnt ? __ldcs(nl + (size_t)(e + t) * DS_SWEEP_THREADS) : 0u;
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++)
+        if (e + t < cnt) F.pair(a, T, S, sb + (int)(ent[t] & DS_SLOT_MASK), (int)(ent[t] >> DS_OFS_SHIFT));
+    }
+    if (act) F.store(a, i);
   }
 }
 
@@ -189,12 +276,16 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 
 template <int CAP>
 static void launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
-  if (what == 0) {
-    if (hpp) k_density32<true, 0, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_density32<false, 0, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  const int n = a.nchunks, t = DS_SWEEP_THREADS;
+  if (what == 0 && a.nbl) {
+    if (hpp) k_density32<true, 0, CAP, true><<<n, t, 0, s>>>(a);
+    else k_density32<false, 0, CAP, true><<<n, t, 0, s>>>(a);
+  } else if (what == 0) {
+    if (hpp) k_density32<true, 0, CAP, false><<<n, t, 0, s>>>(a);
+    else k_density32<false, 0, CAP, false><<<n, t, 0, s>>>(a);
   } else {
-    if (hpp) k_density32<true, 1, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_density32<false, 1, CAP><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    if (hpp) k_density32<true, 1, CAP, false><<<n, t, 0, s>>>(a);
+    else k_density32<false, 1, CAP, false><<<n, t, 0, s>>>(a);
   }
 }
 
@@ -204,13 +295,19 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
   else launch_density32<32>(a, hpp, what, s);
 }
 
+// With recorded lists: the list kernel, then the walk over overflowed chunks.
 void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) {
   if (!a.nchunks) return;
+  const int n = a.nchunks, t = DS_SWEEP_THREADS;
+  if (a.nbl) {
+    if (hpp) k_force32_list<true><<<n, t, 0, s>>>(a);
+    else k_force32_list<false><<<n, t, 0, s>>>(a);
+  }
   if (depth >= 64) {
-    if (hpp) k_force32<true, 64><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_force32<false, 64><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    if (hpp) k_force32<true, 64><<<n, t, 0, s>>>(a);
+    else k_force32<false, 64><<<n, t, 0, s>>>(a);
   } else {
-    if (hpp) k_force32<true, 32><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-    else k_force32<false, 32><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+    if (hpp) k_force32<true, 32><<<n, t, 0, s>>>(a);
+    else k_force32<false, 32><<<n, t, 0, s>>>(a);
   }
 }

@@ -95,6 +95,7 @@ class Params:
     cfl: float = 0.3
     stencil: int = 1      # cells searched on each side: 1 (the reference's 27 cells) or 2 (125 cells)
     list_depth: int = 0   # FP32 sweeps: candidate-list entries per thread (0 -> 32; 64)
+    force_list: int = 0   # FP32: recorded force neighbours per gas particle (0 -> 256; -1 -> off)
     precision: str = "fp64"  # "fp64" or "fp32" (FP32 neighbour sums, FP64 state/IDIC)
     mode: Mode = field(default_factory=Mode)
 
@@ -155,7 +156,7 @@ def parse_init_txt(text: str) -> Params:
             setattr(P.mode, key[5:], val.lower() in ("1", "true", "yes", "on"))
         elif key in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             setattr(P, key, [float(v) for v in val.replace(",", " ").split()])
-        elif key in ("n_dust", "stencil", "list_depth"):
+        elif key in ("n_dust", "stencil", "list_depth", "force_list"):
             setattr(P, key, int(val))
         elif key == "precision":
             P.precision = val
@@ -182,6 +183,7 @@ def write_init_txt(P: Params, extensions: bool = True) -> str:
         out.append(f"n_dust = {P.n_dust}")
         out.append(f"stencil = {P.stencil}")
         out.append(f"list_depth = {P.list_depth}")
+        out.append(f"force_list = {P.force_list}")
         for k in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             out.append(f"{k} = " + " ".join(repr(float(v)) for v in getattr(P, k)))
         out.append(f"precision = {P.precision}")

@@ -57,7 +57,12 @@ def memory_estimate(P: Params, species: List[Species]) -> int:
     n = sum(s.n for s in species)
     ncells, nidic = grid_sizes(P)
     ns = 1 + P.n_dust
-    return int(n * BYTES_PER_PARTICLE + ns * (ncells + 2) * BYTES_PER_KEY + ns * (nidic + 2) * BYTES_PER_IDIC_KEY)
+    b = n * BYTES_PER_PARTICLE + ns * (ncells + 2) * BYTES_PER_KEY + ns * (nidic + 2) * BYTES_PER_IDIC_KEY
+    if P.precision == "fp32" and P.force_list != -1:
+        # recorded force neighbours: cap entries for every slot of the gas chunks
+        cap = P.force_list if P.force_list > 0 else 256
+        b += -(-species[0].n // 128) * 128 * (4 * cap + 4) + -(-species[0].n // 128)
+    return int(b)
 
 
 @dataclasses.dataclass
@@ -105,6 +110,10 @@ class Server:
         P.precision = self.precision
         return P
 
+    def estimate(self, r: Request) -> int:
+        """Device bytes the request takes in this server's batch."""
+        return memory_estimate(self._params(r), r.species)
+
     def run(self, requests: List[Request], on_epoch: Optional[Callable] = None) -> List[Result]:
         pending = sorted(requests, key=lambda r: r.arrival)
         queue: List[Request] = []
@@ -135,10 +144,13 @@ class Server:
                     else:
                         keep.append((t, r))
             # admit waiting requests within the memory budget
-            used = sum(memory_estimate(self._params(r), r.species) for _, r in keep)
+            used = sum(self.estimate(r) for _, r in keep)
             joined = []
             while queue and len(keep) + len(joined) < self.max_tubes:
-                need = memory_estimate(self._params(queue[0]), queue[0].species)
+                need = self.estimate(queue[0])
+                if need > self.budget:
+                    raise ValueError(f"request {queue[0].rid} needs ~{need} device bytes, more than the "
+                                     f"budget of {self.budget:.0f}")
                 if used + need > self.budget:
                     break
                 r = queue.pop(0)

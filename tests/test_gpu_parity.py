@@ -153,6 +153,25 @@ def test_fp32_path_against_fp64_oracle():
     assert np.abs(gpu[1].vx - O.species[1].vx).mean() / vscale < 1e-4
 
 
+@pytest.mark.parametrize("cap", [0, 100, 8])
+def test_fp32_force_lists_equal_walk(cap):
+    """The FP32 force sweep over the neighbours recorded by the density sweep
+    equals the force sweep's own cell walk bit for bit: every chunk listed
+    (0 -> 256 entries), listed and walked chunks mixed (100: interior gas has
+    ~80 neighbours, gas at the contact and in the shock more), every chunk
+    walked (8)."""
+    P, sp = small_tube()
+    P.precision = "fp32"
+    Pw = P.copy()
+    Pw.force_list = -1
+    walk, tw = run_gpu(Pw, sp, 8)
+    Pl = P.copy()
+    Pl.force_list = cap
+    listed, tl = run_gpu(Pl, sp, 8)
+    assert tw == tl
+    compare_exact(listed, walk, f"force_list={cap}")
+
+
 def test_batched_tubes_equal_single_runs():
     cases = [small_tube(eps=1.0, t_s=1e-3), small_tube(eps=0.1, t_s=1e-2, rho_R=0.25, p_R=0.2),
              small_tube(dx_left=1 / 48, Ly=0.375, eps=3.0, t_s=3e-4)]

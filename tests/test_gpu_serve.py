@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from dustyshock3d_gb300 import ic
-from dustyshock3d_gb300.serve import Request, Server, memory_estimate, run_alone
+from dustyshock3d_gb300.serve import Request, Server, run_alone
 
 pytestmark = pytest.mark.gpu
 
@@ -38,7 +38,7 @@ def test_mix_equals_alone(precision):
 
 def test_budget_admits_one_at_a_time():
     reqs = _requests()[:3]
-    one = max(memory_estimate(r.params, r.species) for r in reqs)
+    one = max(Server(precision="fp32").estimate(r) for r in reqs)
     server = Server(budget_bytes=1.2 * one, epoch_steps=4, precision="fp32")
     results = server.run(reqs)
     assert len(results) == 3

@@ -1,8 +1,9 @@
 """Host-side logic of the server and the batch generator (no GPU)."""
 import numpy as np
+import pytest
 
 from dustyshock3d_gb300 import ic
-from dustyshock3d_gb300.serve import grid_sizes, memory_estimate, poisson_requests
+from dustyshock3d_gb300.serve import Server, grid_sizes, memory_estimate, poisson_requests
 from oracle.oracle import OracleState
 
 
@@ -38,3 +39,22 @@ def test_batch_distributions():
     assert 5 <= min(x["p_ratio"] for x in d) and max(x["p_ratio"] for x in d) <= 20
     e = np.log10([x["eps"] for x in d])
     assert -2 <= e.min() and e.max() <= 1 and abs(np.median(e) + 0.5) < 0.1
+
+
+def test_fp32_estimate_counts_force_lists():
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25))
+    P.precision = "fp32"
+    on = memory_estimate(P, sp)
+    P.force_list = -1
+    off = memory_estimate(P, sp)
+    assert on - off >= sp[0].n * 4 * 256
+
+
+def test_request_larger_than_budget_is_refused():
+    """A request that cannot fit even an empty server raises instead of
+    waiting for room that never comes (no GPU work happens before)."""
+    mk = lambda rng: ic.dusty_sod_tube(dx_left=1 / 32, Ly=0.25, x_range=(-0.25, 0.25))  # noqa: E731
+    reqs = poisson_requests(1e6, 2, 3, mk)
+    server = Server(budget_bytes=0.5 * Server(precision="fp32").estimate(reqs[0]), precision="fp32")
+    with pytest.raises(ValueError, match="budget"):
+        server.run(reqs)
