@@ -6,6 +6,7 @@
 // the IDIC cell algebra on the host.  Here one step is ~25 launches on one
 // stream with no host work and no copies; the sequence is captured once into a
 // CUDA graph per buffer parity and replayed.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>

@@ -42,15 +42,6 @@ __global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
 // multiplies instead of FP64 divisions (GB300's FP64 divide is ~20x an FP32
 // multiply-add); periodic axes clamped.  Every cell index of the FP32 path
 // comes from here or from the sorted keys, so they are consistent.
-__device__ __forceinline__ void fast_proper_cell(const TubeDesc &T, double x, double y, double z, int &ix, int &iy,
-                                                 int &iz) {
-  ix = (int)floor((x - T.ox) * T.inv_wx);
-  iy = (int)floor((y - T.oy) * T.inv_wy);
-  iz = (int)floor((z - T.oz) * T.inv_wz);
-  if (T.mode & M_PER_Y) { iy = iy < 0 ? 0 : iy; iy = iy >= T.ny ? T.ny - 1 : iy; }
-  if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
-}
-
 __device__ __forceinline__ int fast_idic_cell(const TubeDesc &T, double x, double y, double z) {
   const int ix = (int)floor((x - T.ox) * T.inv_aw);
   const int iy = (int)floor((y - T.oy) * T.inv_aw);
@@ -76,7 +67,7 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
     int local;
     if (FAST && (T.mode & M_GRID_PROPER)) {
       int ix, iy, iz;
-      fast_proper_cell(T, st.x[i], st.y[i], st.z[i], ix, iy, iz);
+      ds_fast_proper_cell(T, st.x[i], st.y[i], st.z[i], ix, iy, iz);
       const bool in = ix >= 0 && ix < T.nx && iy >= 0 && iy < T.ny && iz >= 0 && iz < T.nz;
       local = in ? ix + iy * T.sy + iz * T.sz : T.ncells + 1;
     } else {
@@ -131,7 +122,7 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
         iy = (local / T.nx) % T.ny;
         iz = local / (T.nx * T.ny);
       } else if (FAST) {
-        fast_proper_cell(T, x, y, z, ix, iy, iz);
+        ds_fast_proper_cell(T, x, y, z, ix, iy, iz);
       } else {
         ds_proper_cell(T, x, y, z, ix, iy, iz);
       }

@@ -152,6 +152,17 @@ __device__ __forceinline__ void ds_proper_cell(const TubeDesc &T, double x, doub
   if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
 }
 
+// Proper cell from the reciprocal cell widths (FP32 path: no FP64 divisions;
+// the FP32 path's keys, and so its sorted cells, come from this).
+__device__ __forceinline__ void ds_fast_proper_cell(const TubeDesc &T, double x, double y, double z, int &ix,
+                                                    int &iy, int &iz) {
+  ix = (int)floor((x - T.ox) * T.inv_wx);
+  iy = (int)floor((y - T.oy) * T.inv_wy);
+  iz = (int)floor((z - T.oz) * T.inv_wz);
+  if (T.mode & M_PER_Y) { iy = iy < 0 ? 0 : iy; iy = iy >= T.ny ? T.ny - 1 : iy; }
+  if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
+}
+
 // Raw neighbour-cell key, kernel.cu:1949 / IDIC.h:28 (int() truncation).
 // Proper grid: -1 when an axis is out of range.
 __device__ __forceinline__ int ds_raw_key(const TubeDesc &T, double x, double y, double z) {
@@ -198,6 +209,21 @@ __device__ __forceinline__ void ds_stencil_init(const TubeDesc &T, double x, dou
   } else {
     s.ni = 0;
     ds_proper_cell(T, x, y, z, s.ix, s.iy, s.iz);
+  }
+}
+
+// Own cell of a slot on the FP32 path: decoded from its sorted key -- the cell
+// its FP32 coordinates are relative to -- or, for a particle outside the grid
+// (orphan bucket), from its position as the FP32 keys compute it.
+__device__ __forceinline__ void ds_stencil_from_key(const TubeDesc &T, int local, double x, double y, double z,
+                                                    Stencil &s) {
+  s.ni = 0;
+  if (local < T.ncells) {
+    s.ix = local % T.nx;
+    s.iy = (local / T.nx) % T.ny;
+    s.iz = local / (T.nx * T.ny);
+  } else {
+    ds_fast_proper_cell(T, x, y, z, s.ix, s.iy, s.iz);
   }
 }
 
@@ -264,6 +290,19 @@ __device__ __forceinline__ void ds_shift32(const TubeDesc &T, const Stencil &S, 
   if (T.mode & M_PER_Z) {
     const int cz = S.iz + g;
     sz = cz < 0 ? -f.Lz : (cz >= T.nz ? f.Lz : 0.0f);
+  }
+}
+
+// FP32 shifts (k wx, l wy, g wz) of the 125 offset codes (k, l, g) in
+// [-2, 2]^3, formed as ds_shift32 forms them for cell-relative coordinates
+// (every tube on the FP32 path has them); one table per block, for the
+// tube of its chunk.
+#define DS_NOFS5 125
+__device__ __forceinline__ void ds_fill_shift_table(const TubeDesc &T, float4 *tab) {
+  const Shift32 f = ds_shift32_init(T);
+  for (int o5 = threadIdx.x; o5 < DS_NOFS5; o5 += blockDim.x) {
+    const int k = o5 / 25 - 2, l = (o5 / 5) % 5 - 2, g = o5 % 5 - 2;
+    tab[o5] = make_float4((float)k * f.wx, (float)l * f.wy, (float)g * f.wz, 0.0f);
   }
 }
 

@@ -62,13 +62,17 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
 // order.  A chunk with a particle beyond nbl_cap entries is flagged; the force
 // sweep walks that chunk.
 template <bool HPP, int WHAT, int CAP, bool LIST>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 6 : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
+__global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 7 : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
+  __shared__ float4 shtab[DS_NOFS5];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const bool valid = i < ch.end && a.tstate[ch.tube].active;
     const TubeDesc &T = a.tubes[ch.tube];
+    __syncthreads();  // the previous chunk's table is no longer read
+    ds_fill_shift_table(T, shtab);
+    __syncthreads();
     const int s = ch.species;
     const int ind = valid ? a.st.ind[i] : 1;
     const bool upd = valid && ind == 0;
@@ -80,13 +84,11 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 6 : (WHAT ? 9 : 8)) k
     }
     double rho = valid ? a.st.rho[i] : 0.0;
     if (zero) rho = 0.0;
-    const double xi = upd ? a.st.x[i] : 0.0, yi = upd ? a.st.y[i] : 0.0, zi = upd ? a.st.z[i] : 0.0;
     const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
     const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
-    const Shift32 f32 = ds_shift32_init(T);
-    Stencil S;
-    ds_stencil_init(T, xi, yi, zi, S);
+    Stencil S{0, 0, 0, 0};
+    if (upd) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
     const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[a.skey[i]]) : (hd <= T.r1_hmax ? 1 : T.stencil);
     const int sb = T.seg_begin[s];
     uint32_t *nl = LIST ? a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x : nullptr;
@@ -104,11 +106,13 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 6 : (WHAT ? 9 : 8)) k
           return r2 < cut2;
         },
         [&](int j, int o5) {
-          float ox, oy, oz;
-          ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
+          const float4 sh = shtab[o5];
           const float4 pj = a.pos32[j];
-          const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
-          if (!LIST || r2 < cut2) sum.add(a.vm32[j].w * w_shape(sqrtf(r2) * inv_h));
+          const float r2 = r2_of(pj.x + (sh.x - pi.x), pj.y + (sh.y - pi.y), pj.z + (sh.z - pi.z));
+          if (!LIST || r2 < cut2) {
+            const float q = r2 > 0.0f ? r2 * rsqrtf(r2) * inv_h : 0.0f;
+            sum.add(a.vm32[j].w * w_shape(q));
+          }
           if (LIST && r2 > 0.0f) {
             if (cnt < a.nbl_cap)
               nl[(size_t)cnt * DS_SWEEP_THREADS] = ((uint32_t)o5 << DS_OFS_SHIFT) | (uint32_t)(j - sb);
@@ -132,7 +136,9 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 6 : (WHAT ? 9 : 8)) k
       // force inputs and the CFL bound in FP32 (the force sweep is FP32)
       const float rhof = (float)rho, pf = (float)p;
       const float csf = sqrtf((float)T.gam * pf / rhof);
-      a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 0.0f);
+      // .w: 1/h of the particle (frozen ones too: they are force partners)
+      const float hown = HPP ? a.pos32[i].w : (float)T.h;
+      a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
       if (upd && (T.mode & M_CFL)) {
         const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
         const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
@@ -148,25 +154,23 @@ template <bool HPP>
 struct ForceSum {
   float4 pi, vmi;
   float hi, inv_hi, ni, mi, rhoi, pti, csi, mpi, alpha, beta, eps;
-  Shift32 f32;
   Kahan Ax, Ay, Az, et;
 
   __device__ __forceinline__ ForceSum(const SweepArgs &a, const TubeDesc &T, int i, bool act) {
     pi = act ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 1.f);
     vmi = act ? a.vm32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 hyi = act ? a.hyd32[i] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const float4 hyi = act ? a.hyd32[i] : make_float4(0.f, 0.f, 1.f, 1.f);
     hi = HPP ? pi.w : (float)T.h;
-    inv_hi = 1.0f / hi;
+    inv_hi = hyi.w;
     ni = (float)(1.0 / 3.14159265) * inv_hi * inv_hi * inv_hi * inv_hi;
     mi = vmi.w;
     rhoi = hyi.z;
     pti = hyi.y;
     csi = hyi.x;
-    mpi = act ? (float)(a.st.m[i] * a.st.p[i] / (a.st.rho[i] * a.st.rho[i])) : 0.0f;
+    mpi = mi * pti;  // m_i p_i / rho_i^2
     alpha = (float)T.alpha;
     beta = (float)T.beta;
     eps = (float)T.eps;
-    f32 = ds_shift32_init(T);
   }
 
   // the force sweep's screen: 0 < r < 2 max(h_i, h_j)
@@ -176,28 +180,26 @@ struct ForceSum {
     return (r2 < 4.0f * hc * hc) && (r2 > 0.0f);
   }
 
-  __device__ __forceinline__ void pair(const SweepArgs &a, const TubeDesc &T, const Stencil &S, int j, int o5) {
-    float ox, oy, oz;
-    ds_rel_shift32(T, S, f32, pi, o5, ox, oy, oz);
+  // sh: the FP32 shift of the entry's cell (shift table), as the screen saw it
+  __device__ __forceinline__ void pair(const SweepArgs &a, const float4 &sh, int j) {
     const float4 pj = a.pos32[j];
-    const float dx = pj.x + ox, dy = pj.y + oy, dz = pj.z + oz;
+    const float dx = pj.x + (sh.x - pi.x), dy = pj.y + (sh.y - pi.y), dz = pj.z + (sh.z - pi.z);
     const float r2 = r2_of(dx, dy, dz);
     const float inv_d = rsqrtf(r2);
     const float dist = r2 * inv_d;
-    const float hj = HPP ? pj.w : hi;
     const float4 vmj = a.vm32[j];
     const float4 hyj = a.hyd32[j];
-    const float hh = HPP ? 0.5f * (hi + hj) : hi;
+    const float hh = HPP ? 0.5f * (hi + pj.w) : hi;
     const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
     float F = 0.0f;
     if (nu < 0.0f) {
       const float Cnu = 0.5f * (csi + hyj.x);
-      const float mu = hh * nu / (r2 + eps * hh * hh);
-      F = (-alpha * Cnu * mu + beta * mu * mu) / (0.5f * (rhoi + hyj.z));
+      const float mu = __fdividef(hh * nu, r2 + eps * hh * hh);
+      F = __fdividef(-alpha * Cnu * mu + beta * mu * mu, 0.5f * (rhoi + hyj.z));
     }
     float dWr = ni * dw_shape(dist * inv_hi);
     if (HPP) {
-      const float inv_hj = 1.0f / hj;
+      const float inv_hj = hyj.w;
       const float nj = (float)(1.0 / 3.14159265) * inv_hj * inv_hj * inv_hj * inv_hj;
       dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
     }
@@ -222,22 +224,25 @@ struct ForceSum {
 template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
+  __shared__ float4 shtab[DS_NOFS5];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     if (a.nbl && !a.nbl_walk[c]) continue;
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
+    __syncthreads();
+    ds_fill_shift_table(T, shtab);
+    __syncthreads();
     const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int s = ch.species;
-    const double xi = act ? a.st.x[i] : 0.0, yi = act ? a.st.y[i] : 0.0, zi = act ? a.st.z[i] : 0.0;
     ForceSum<HPP> F(a, T, i, act);
-    Stencil S;
-    ds_stencil_init(T, xi, yi, zi, S);
+    Stencil S{0, 0, 0, 0};
+    if (act) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
     ds_walk<CAP>(
         T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) { return F.screen(a.pos32[j], ox, oy, oz); },
-        [&](int j, int o5) { F.pair(a, T, S, j, o5); });
+        [&](int j, int o5) { F.pair(a, shtab[o5], j); });
     if (act) F.store(a, i);
   }
 }
@@ -247,16 +252,18 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
+  __shared__ float4 shtab[DS_NOFS5];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     if (a.nbl_walk[c]) continue;
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
+    __syncthreads();
+    ds_fill_shift_table(T, shtab);
+    __syncthreads();
     const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int sb = T.seg_begin[ch.species];
     ForceSum<HPP> F(a, T, i, act);
-    Stencil S;
-    ds_stencil_init(T, act ? a.st.x[i] : 0.0, act ? a.st.y[i] : 0.0, act ? a.st.z[i] : 0.0, S);
     const int cnt = act ? a.nbl_cnt[i] : 0;
     const int cnt_w = __reduce_max_sync(FULL, cnt);
     const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
@@ -266,7 +273,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
       for (int t = 0; t < DS_PIECE; t++) ent[t] = e + t < cnt ? __ldcs(nl + (size_t)(e + t) * DS_SWEEP_THREADS) : 0u;
 #pragma unroll
       for (int t = 0; t < DS_PIECE; t++)
-        if (e + t < cnt) F.pair(a, T, S, sb + (int)(ent[t] & DS_SLOT_MASK), (int)(ent[t] >> DS_OFS_SHIFT));
+        if (e + t < cnt) F.pair(a, shtab[ent[t] >> DS_OFS_SHIFT], sb + (int)(ent[t] & DS_SLOT_MASK));
     }
     if (act) F.store(a, i);
   }

@@ -59,9 +59,11 @@ def memory_estimate(P: Params, species: List[Species]) -> int:
     ns = 1 + P.n_dust
     b = n * BYTES_PER_PARTICLE + ns * (ncells + 2) * BYTES_PER_KEY + ns * (nidic + 2) * BYTES_PER_IDIC_KEY
     if P.precision == "fp32" and P.force_list != -1:
-        # recorded force neighbours: cap entries for every slot of the gas chunks
+        # recorded force neighbours: cap entries for every slot of the gas
+        # chunks, a count per slot, a flag per chunk
         cap = P.force_list if P.force_list > 0 else 256
-        b += -(-species[0].n // 128) * 128 * (4 * cap + 4) + -(-species[0].n // 128)
+        chunks = -(-species[0].n // 128)
+        b += chunks * 128 * 4 * cap + chunks + 4 * n
     return int(b)
 
 
