@@ -15,7 +15,7 @@ Reported (one JSON line from rank 0):
   e2e        the same metric through the C ABI with host buffers: every step
              uploads the full particle state from pinned memory, steps once,
              and downloads the full state
-  roofline   the force sweep (dominant kernel): compulsory bytes / duration
+  roofline   the gas density sweep (dominant kernel): compulsory bytes / duration
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on a bounded sample
 
 --impl reference times the reference algorithm on the host cores (the oracle,
@@ -39,7 +39,7 @@ sys.path.insert(0, ROOT)
 
 # Batched and served workloads (not the default line): 64 seeded uneven tubes,
 # and a Poisson stream of such tubes under a 150 GB budget.
-EXTRA_WORKLOADS = ("batch64", "serve")
+EXTRA_WORKLOADS = ("batch64", "serve", "accuracy_720k")
 
 WORKLOADS = {
     # name: (dx_left, Ly, description)
@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--t-end", type=float, default=0.2, help="accuracy_720k: end time of every run")
     return ap.parse_args()
 
 
@@ -153,6 +154,25 @@ def dist_max(dist, v):
 def barrier(dist):
     if dist is not None:
         dist.barrier()
+
+
+def replica_rate(dist, ws, n, steps, ms):
+    """Whole-job particle-steps/s of ws ranks that each advanced n particles
+    for `steps` steps in `ms` milliseconds: the slowest rank sets the time."""
+    return ws * n * steps / (dist_max(dist, ms) * 1e-3)
+
+
+def balanced_shards(sizes, ws):
+    """Independent tubes split over ws ranks, largest first onto the least
+    loaded rank (deterministic; ties to the lower rank).  Returns one sorted
+    index list per rank."""
+    load = [0] * ws
+    out = [[] for _ in range(ws)]
+    for i in sorted(range(len(sizes)), key=lambda i: (-sizes[i], i)):
+        r = min(range(ws), key=lambda r: (load[r], r))
+        load[r] += sizes[i]
+        out[r].append(i)
+    return [sorted(o) for o in out]
 
 
 # ---------------------------------------------------------------------------
@@ -248,6 +268,15 @@ def profile_traffic(path):
     except OSError:
         pass
     return None
+
+
+def density_bytes_per_particle(hpp: bool) -> int:
+    """Compulsory bytes of one FP32 gas density launch per gas particle, each
+    array read or written once, not counting the recorded force neighbours
+    (4 bytes per entry, added by the caller): read pos32, vm32 (32), h (8,
+    per-particle h), rho, p, e (24), vx, vy, vz (24, CFL bound), Ind and the
+    own cell key (8); write rho, p (16), hyd32 (16), the list count (4)."""
+    return 32 + (8 if hpp else 0) + 24 + 24 + 8 + 16 + 16 + 4
 
 
 def force_bytes_per_particle(fp32: bool, hpp: bool) -> int:
@@ -346,11 +375,15 @@ def run_ours(args):
     S.step(args.warmup)
     barrier(dist)
     total_ms, phase = S.step_timed(args.steps)
+    value = replica_rate(dist, ws, n, args.steps, total_ms)
     total_ms = dist_max(dist, total_ms)
     kps = S.kernels_per_step()
     g32 = S.get_species(0, 0)
     d32 = S.get_species(0, 1)
     t32 = S.time(0)
+    # recorded force neighbours of the final state (0 < r < 2 max(h_i, h_j),
+    # counted by the parity hook; after the timed region)
+    list_entries = int(S.debug_cells(0, 0)["nnb"][g32.ind == 0].sum())
     S.close()
 
     fp64 = None
@@ -385,17 +418,18 @@ def run_ours(args):
 
     if rank != 0:
         return 0
-    value = ws * n * args.steps / (total_ms * 1e-3)
     peak, peak_kind = peak_hbm()
-    force_ms = phase[2] / args.steps
-    bpp = force_bytes_per_particle(True, P.mode.h_per_particle)
-    achieved = bpp * n_gas / (force_ms * 1e-3) / 1e9
-    tr = profile_traffic(os.path.join(ROOT, "profiles", "force32_dusty_sod_720k.txt"))
-    roof = {"kernel": "k_force32 (force + energy-rate sweep, FP32)", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+    dens_ms = phase[1] / args.steps
+    alg = density_bytes_per_particle(P.mode.h_per_particle) * n_gas + 4 * list_entries
+    achieved = alg / (dens_ms * 1e-3) / 1e9
+    tr = profile_traffic(os.path.join(ROOT, "profiles", "density32_dusty_sod_720k.txt"))
+    roof = {"kernel": "k_density32 (gas density + EOS + force-list record, FP32)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": None if tr is None else tr * n_gas,
-            "algorithmic_bytes_per_launch": bpp * n_gas, "avg_launch_ms": force_ms,
-            "note": "the sweep is FP32-issue bound, not HBM bound (candidates from 27 cells per particle)"}
+            "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dens_ms,
+            "list_entries_per_launch": list_entries,
+            "note": "issue-bound, not HBM-bound: every particle screens the candidates of 27 (or 125) cells "
+                    "in FP32; traffic from the committed ncu capture of this workload"}
     cpu = None
     if not args.no_cpu_baseline:
         v, sample, _ = time_cpu(name, 3)
@@ -417,10 +451,16 @@ def run_ours(args):
 
 
 def run_batch(args):
-    """64 uneven tubes (seeded) advanced together, FP32, autotuned."""
+    """64 uneven tubes (seeded) advanced together, FP32, autotuned.  With N
+    ranks the tubes are split over the GPUs (balanced by particle count; the
+    tubes are independent, so no collective touches the data path)."""
     from dustyshock3d_gb300 import ic, tune
     from dustyshock3d_gb300.solver import Solver
-    tubes = ic.batch_tubes(seed=args.seed, n_tubes=64)
+    ws, rank, dist = dist_setup()
+    all_tubes = ic.batch_tubes(seed=args.seed, n_tubes=64)
+    shards = balanced_shards([sum(s.n for s in sp) for _, sp in all_tubes], ws)
+    tubes = [all_tubes[i] for i in shards[rank]]
+    n_all = sum(sum(s.n for s in sp) for _, sp in all_tubes)
     choice, log = tune.tune(tubes, sample=8)
     ps = []
     for P, _ in tubes:
@@ -434,15 +474,21 @@ def run_batch(args):
         for t, (_, sp) in enumerate(tubes):
             S.set_tube(t, sp)
         S.step(args.warmup)
+        barrier(dist)
         total_ms, phase = S.step_timed(args.steps)
         kps = S.kernels_per_step()
         mem = S.memory_bytes()
     clk = clocks.stop()
-    value = n * args.steps / (total_ms * 1e-3)
-    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
+    total_ms = dist_max(dist, total_ms)
+    if rank != 0:
+        return 0
+    value = n_all * args.steps / (total_ms * 1e-3)
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64", "tubes": 64, "particles": n, "seed": args.seed,
+            "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64", "tubes": 64, "particles": n_all, "seed": args.seed,
+                       "tubes_on_rank0": len(tubes), "particles_on_rank0": n,
                        "autotuned": dataclasses.asdict(choice),
                        "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, ms=d) for a, b, c, d in log],
                        "device_bytes": mem},
@@ -495,6 +541,60 @@ def run_serve(args):
     return 0
 
 
+def run_accuracy(args):
+    """The 720k tube to t_end on the FP64 and the FP32 path for
+    t_s in {1e-1, 1e-2, 1e-3, 1e-4} x eps in {0.01, 1, 10}: L1 error of the
+    FP32 path's gas density, gas and dust x-velocity against the FP64 path
+    (sum |a - b| / sum |b|), and both paths' rates."""
+    import numpy as np
+
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300.solver import Solver
+    ws, rank, dist = dist_setup()
+    if rank != 0:
+        return 0
+    dx, Ly, _ = WORKLOADS["dusty_sod_720k"]
+    rel = lambda a, b: float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))  # noqa: E731
+    clocks = ClockSampler(0)
+    clocks.start()
+    rows = []
+    for t_s in (1e-1, 1e-2, 1e-3, 1e-4):
+        for eps in (0.01, 1.0, 10.0):
+            P, sp = ic.dusty_sod_tube(dx_left=dx, Ly=Ly, eps=eps, t_s=t_s, t_end=args.t_end)
+            n = sum(q.n for q in sp)
+            res = {}
+            for prec in ("fp64", "fp32"):
+                Q = P.copy()
+                Q.precision = prec
+                with Solver(Q) as S:
+                    S.set_tube(0, sp)
+                    ms_tot, groups = 0.0, 0
+                    while S.time(0)[0] < Q.T_end and groups < 2000:  # bounded: 20000 steps
+                        ms, _ = S.step_timed(10)
+                        ms_tot += ms
+                        groups += 1
+                    Tm, _, nstep = S.time(0)
+                    res[prec] = (S.get_species(0, 0), S.get_species(0, 1), Tm, nstep, ms_tot)
+            g64, d64, T64, n64, ms64 = res["fp64"]
+            g32, d32, T32, n32, ms32 = res["fp32"]
+            rows.append({"t_s": t_s, "eps": eps, "t": T32, "steps_fp32": n32, "steps_fp64": n64,
+                         "l1_rho_gas": rel(g32.rho, g64.rho), "l1_v_gas": rel(g32.vx, g64.vx),
+                         "l1_v_dust": rel(d32.vx, d64.vx),
+                         "fp32_particle_steps_per_s": n * n32 / (ms32 * 1e-3),
+                         "fp64_particle_steps_per_s": n * n64 / (ms64 * 1e-3)})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    clk = clocks.stop()
+    line = {"metric": "l1 error, fp32 path vs fp64 path", "workload": "accuracy_720k", "t_end": args.t_end,
+            "particles": n, "rows": rows,
+            "max_l1_rho_gas": max(r["l1_rho_gas"] for r in rows),
+            "max_l1_v_gas": max(r["l1_v_gas"] for r in rows),
+            "max_l1_v_dust": max(r["l1_v_dust"] for r in rows),
+            "note": "rates include up to 9 steps after t_end that do no work (steps run in groups of 10)",
+            "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -503,6 +603,8 @@ def main():
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "accuracy_720k":
+        return run_accuracy(args)
     return run_ours(args)
 
 

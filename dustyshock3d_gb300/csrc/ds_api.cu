@@ -320,10 +320,10 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
     if (fp32) ds_launch_density32(ad, c->any_hpp, 1, depth, s);
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
   }
+  if (ev) cudaEventRecord(ev[2], s);
   DevState st = c->buf[c->parity].view();
   ds_launch_tstop(c->d_tubes, c->d_tstate, c->d_ch_dust, (int)c->ch_dust.size(), st, c->slot_of_pid, c->d_flags, s);
   ds_launch_dt(c->d_tubes, c->d_tstate, c->ntubes, s);
-  if (ev) cudaEventRecord(ev[2], s);
   if (fp32) ds_launch_force32(ag, c->any_hpp, depth, s);
   else ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
   if (ev) cudaEventRecord(ev[3], s);

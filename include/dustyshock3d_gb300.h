@@ -198,8 +198,9 @@ ds_status ds_conservation(ds_ctx *c, int tube, double *out6);
 /* Runs nsteps steps back to back (the graph's kernels, launched one by one)
  * with CUDA events between phases on the context's stream; returns the total
  * device time and the per-phase sums in milliseconds: [0] keys, sort, reorder,
- * cell ranges, IDIC-key sort; [1] density, EOS, t_stop, step size; [2] force
- * sweep; [3] IDIC reduce + solve, relax, move, energy. */
+ * cell ranges, IDIC-key sort; [1] density sweeps with the EOS (and, on the
+ * FP32 path, the force neighbour lists); [2] t_stop, step size, force sweep;
+ * [3] IDIC reduce + solve, relax, move, energy. */
 ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms);
 
 /* Number of kernels one step launches (the library's own kernels). */
