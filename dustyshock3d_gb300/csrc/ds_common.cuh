@@ -359,7 +359,9 @@ __device__ __forceinline__ void ds_decode_ofs(int o5, int &k, int &l, int &g) {
 // particle (act false) take part with empty stencils.
 #define DS_SWEEP_THREADS 128
 #define DS_LIST_CAP 32  // entries per thread in the shared list
+#ifndef DS_PIECE
 #define DS_PIECE 4      // candidates screened together (loads in flight); measured best of 1-16
+#endif
 #define DS_OFS_SHIFT 25
 #define DS_SLOT_MASK ((1u << DS_OFS_SHIFT) - 1u)
 

@@ -61,8 +61,11 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
 // exactly the pairs the force sweep's own walk would accept, in its visiting
 // order.  A chunk with a particle beyond nbl_cap entries is flagged; the force
 // sweep walks that chunk.
+#ifndef DS_DENS_LIST_MINB
+#define DS_DENS_LIST_MINB 6  // blocks per SM the list-recording density sweep is built for
+#endif
 template <bool HPP, int WHAT, int CAP, bool LIST>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? 7 : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
+__global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   __shared__ float4 shtab[DS_NOFS5];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
@@ -182,13 +185,15 @@ struct ForceSum {
 
   // sh: the FP32 shift of the entry's cell (shift table), as the screen saw it
   __device__ __forceinline__ void pair(const SweepArgs &a, const float4 &sh, int j) {
-    const float4 pj = a.pos32[j];
+    pair(sh, a.pos32[j], a.vm32[j], a.hyd32[j]);
+  }
+
+  // the same with the neighbour's pos32, vm32, hyd32 already loaded
+  __device__ __forceinline__ void pair(const float4 &sh, const float4 &pj, const float4 &vmj, const float4 &hyj) {
     const float dx = pj.x + (sh.x - pi.x), dy = pj.y + (sh.y - pi.y), dz = pj.z + (sh.z - pi.z);
     const float r2 = r2_of(dx, dy, dz);
     const float inv_d = rsqrtf(r2);
     const float dist = r2 * inv_d;
-    const float4 vmj = a.vm32[j];
-    const float4 hyj = a.hyd32[j];
     const float hh = HPP ? 0.5f * (hi + pj.w) : hi;
     const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
     float F = 0.0f;
@@ -249,6 +254,9 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 
 // Force sweep over the recorded lists: no cell walk, no screening; entries in
 // the walk's order, so the sums equal the walk's.
+#ifndef DS_FPIECE
+#define DS_FPIECE 2  // list entries per pipeline stage (measured: 2 beats 4)
+#endif
 template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
@@ -267,13 +275,32 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
     const int cnt = act ? a.nbl_cnt[i] : 0;
     const int cnt_w = __reduce_max_sync(FULL, cnt);
     const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
-    for (int e = 0; e < cnt_w; e += DS_PIECE) {
-      uint32_t ent[DS_PIECE];
+    // software pipeline: the next piece's entries load while this piece's
+    // neighbour data loads, before any of its pair work
+    uint32_t ent[DS_FPIECE];
 #pragma unroll
-      for (int t = 0; t < DS_PIECE; t++) ent[t] = e + t < cnt ? __ldcs(nl + (size_t)(e + t) * DS_SWEEP_THREADS) : 0u;
+    for (int t = 0; t < DS_FPIECE; t++) ent[t] = t < cnt ? __ldcs(nl + (size_t)t * DS_SWEEP_THREADS) : 0u;
+    for (int e = 0; e < cnt_w; e += DS_FPIECE) {
+      float4 pj[DS_FPIECE], vmj[DS_FPIECE], hyj[DS_FPIECE];
 #pragma unroll
-      for (int t = 0; t < DS_PIECE; t++)
-        if (e + t < cnt) F.pair(a, shtab[ent[t] >> DS_OFS_SHIFT], sb + (int)(ent[t] & DS_SLOT_MASK));
+      for (int t = 0; t < DS_FPIECE; t++)
+        if (e + t < cnt) {
+          const int j = sb + (int)(ent[t] & DS_SLOT_MASK);
+          pj[t] = a.pos32[j];
+          vmj[t] = a.vm32[j];
+          hyj[t] = a.hyd32[j];
+        }
+      uint32_t nxt[DS_FPIECE];
+#pragma unroll
+      for (int t = 0; t < DS_FPIECE; t++) {
+        const int q = e + DS_FPIECE + t;
+        nxt[t] = q < cnt ? __ldcs(nl + (size_t)q * DS_SWEEP_THREADS) : 0u;
+      }
+#pragma unroll
+      for (int t = 0; t < DS_FPIECE; t++)
+        if (e + t < cnt) F.pair(shtab[ent[t] >> DS_OFS_SHIFT], pj[t], vmj[t], hyj[t]);
+#pragma unroll
+      for (int t = 0; t < DS_FPIECE; t++) ent[t] = nxt[t];
     }
     if (act) F.store(a, i);
   }
