@@ -72,7 +72,7 @@ struct ds_ctx {
   Chunk *d_ch_all = nullptr, *d_ch_gas = nullptr, *d_ch_dust = nullptr;
   int *d_seg_key0 = nullptr, *d_seg_species = nullptr, *d_seg_orphan = nullptr, *d_tube_cell0 = nullptr;
   int *d_nseg_key0 = nullptr, *d_nseg_tube = nullptr, *d_nseg_species = nullptr;
-  double *hmax = nullptr;
+  unsigned char *cbig = nullptr, *corx = nullptr;  // stencil-radius passes
   unsigned char *krad = nullptr;
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
@@ -292,7 +292,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   ds_launch_cell_start(skey, c->N, c->nkeys, c->cell_start, s);
   c->skey = skey;
   if (c->any_stencil2)
-    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->hmax, c->d_nseg_key0, c->d_nseg_tube,
+    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->cbig, c->corx, c->d_nseg_key0, c->d_nseg_tube,
                           c->d_nseg_species, c->nnseg, c->krad, s);
   c->parity ^= 1;
 }
@@ -419,7 +419,8 @@ ds_status finalize(ds_ctx *c) {
   DA(c->slot_of_pid, N); DA(c->ind_of_pid, N); DA(c->idic_local, N);
   DA(c->cell_start, (size_t)nkeys + 1);
   DA(c->ncand, N); DA(c->nnb, N);
-  DA(c->hmax, (size_t)nkeys);
+  DA(c->cbig, (size_t)nkeys);
+  DA(c->corx, (size_t)nkeys);
   DA(c->krad, (size_t)nkeys);
   CK(cudaMemsetAsync(c->krad, 1, (size_t)nkeys, c->stream));
   DA(c->stage, N);
@@ -804,7 +805,7 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
   *count = 13 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
-           (c->any_stencil2 ? 2 : 0) + (c->nbl ? 1 : 0);
+           (c->any_stencil2 ? 3 : 0) + (c->nbl ? 1 : 0);
   return DS_OK;
 }
 

@@ -541,20 +541,43 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
   }
 }
 
-// Largest h of each cell (every key), for the stencil-radius choice.
-__global__ void k_cell_hmax(const int *cell_start, int nkeys, const double *h, double *hmax) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nkeys) return;
-  double m = 0.0;
-  for (int j = cell_start[k]; j < cell_start[k + 1]; j++) m = fmax(m, h[j]);
-  hmax[k] = m;
+// Stencil radius each cell's force sweep needs: 1 when no particle within R
+// cells (R = the tube's stencil) has h above half the cell width -- every
+// partner within the cut-off is then in the 27 inner cells -- else R.  Three
+// separable passes over the key space: a flag per cell (some h above the
+// limit), its OR over the x window, then over the y-z window (periodic axes
+// wrap).  Reference grids and the orphan buckets keep the tube's stencil.
+__global__ void k_cell_big(const TubeDesc *tubes, const int *cell_start, const int *nseg_key0,
+                           const int *nseg_tube, int nseg, int nkeys, const double *h, unsigned char *big) {
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  if (key >= nkeys) return;
+  const double lim = tubes[nseg_tube[find_seg(nseg_key0, nseg, key)]].r1_hmax;
+  unsigned char b = 0;
+  for (int j = cell_start[key]; j < cell_start[key + 1]; j++) b |= (unsigned char)(h[j] > lim);
+  big[key] = b;
 }
 
-// Stencil radius each cell's force sweep needs: 1 when no particle within two
-// cells has h above half the cell width (every partner within the cut-off is
-// then in the 27 inner cells), else the tube's stencil.
+__global__ void k_cell_or_x(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
+                            const int *nseg_species, int nseg, int nkeys, const unsigned char *big,
+                            unsigned char *orx) {
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  if (key >= nkeys) return;
+  const int sg = find_seg(nseg_key0, nseg, key);
+  const TubeDesc &T = tubes[nseg_tube[sg]];
+  const int local = key - T.key_base[nseg_species[sg]];
+  if (T.stencil == 1 || local >= T.ncells || !(T.mode & M_GRID_PROPER)) {
+    orx[key] = big[key];
+    return;
+  }
+  const int ix = local % T.nx, R = T.stencil;
+  unsigned char b = 0;
+  for (int k = -R; k <= R; k++)
+    if (ix + k >= 0 && ix + k < T.nx) b |= big[key + k];
+  orx[key] = b;
+}
+
 __global__ void k_cell_radius(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
-                              const int *nseg_species, int nseg, int nkeys, const double *hmax,
+                              const int *nseg_species, int nseg, int nkeys, const unsigned char *orx,
                               unsigned char *krad) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
@@ -566,23 +589,19 @@ __global__ void k_cell_radius(const TubeDesc *tubes, const int *nseg_key0, const
   if (local >= T.ncells || !(T.mode & M_GRID_PROPER)) { krad[key] = (unsigned char)T.stencil; return; }
   const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
   const int R = T.stencil;
-  double H = 0.0;
-  for (int k = -R; k <= R; k++) {
-    const int cx = ix + k;
-    if (cx < 0 || cx >= T.nx) continue;
-    for (int l = -R; l <= R; l++) {
-      int cy = iy + l;
-      if (T.mode & M_PER_Y) cy = (cy + T.ny) % T.ny;
-      else if (cy < 0 || cy >= T.ny) continue;
-      for (int g = -R; g <= R; g++) {
-        int cz = iz + g;
-        if (T.mode & M_PER_Z) cz = (cz + T.nz) % T.nz;
-        else if (cz < 0 || cz >= T.nz) continue;
-        H = fmax(H, hmax[kb + cx + cy * T.sy + cz * T.sz]);
-      }
+  unsigned char b = 0;
+  for (int l = -R; l <= R; l++) {
+    int cy = iy + l;
+    if (T.mode & M_PER_Y) cy = (cy + T.ny) % T.ny;
+    else if (cy < 0 || cy >= T.ny) continue;
+    for (int g = -R; g <= R; g++) {
+      int cz = iz + g;
+      if (T.mode & M_PER_Z) cz = (cz + T.nz) % T.nz;
+      else if (cz < 0 || cz >= T.nz) continue;
+      b |= orx[kb + ix + cy * T.sy + cz * T.sz];
     }
   }
-  krad[key] = H <= T.r1_hmax ? 1 : (unsigned char)R;
+  krad[key] = b ? (unsigned char)R : 1;
 }
 
 __global__ void k_fill(double *a, int n, double v) {
@@ -676,10 +695,11 @@ void ds_launch_iota(int *a, int n, cudaStream_t s) {
   if (n > 0) k_iota<<<blocks_for(n, 256), 256, 0, s>>>(a, n);
 }
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, const double *h,
-                           double *hmax, const int *nseg_key0, const int *nseg_tube, const int *nseg_species,
-                           int nseg, unsigned char *krad, cudaStream_t s) {
+                           unsigned char *big, unsigned char *orx, const int *nseg_key0, const int *nseg_tube,
+                           const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s) {
   if (nkeys <= 0) return;
-  k_cell_hmax<<<blocks_for(nkeys, 256), 256, 0, s>>>(cell_start, nkeys, h, hmax);
-  k_cell_radius<<<blocks_for(nkeys, 128), 128, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys,
-                                                      hmax, krad);
+  const int b = blocks_for(nkeys, 256);
+  k_cell_big<<<b, 256, 0, s>>>(tubes, cell_start, nseg_key0, nseg_tube, nseg, nkeys, h, big);
+  k_cell_or_x<<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, big, orx);
+  k_cell_radius<<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, orx, krad);
 }
