@@ -72,7 +72,7 @@ struct ds_ctx {
   Chunk *d_ch_all = nullptr, *d_ch_gas = nullptr, *d_ch_dust = nullptr;
   int *d_seg_key0 = nullptr, *d_seg_species = nullptr, *d_seg_orphan = nullptr, *d_tube_cell0 = nullptr;
   int *d_nseg_key0 = nullptr, *d_nseg_tube = nullptr, *d_nseg_species = nullptr;
-  unsigned char *cbig = nullptr, *corx = nullptr;  // stencil-radius passes
+  double *cwa = nullptr, *cwb = nullptr;  // stencil-radius passes (h maxima per key)
   unsigned char *krad = nullptr;
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
@@ -201,9 +201,10 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   // FP32 screen slack: rounding of |coordinate| <= L (or <= 2 cell widths when
   // cell-relative) in each of the two operands, with a 5x margin
   T.pre_abs = (float)(1e-6 * (proper ? 4.0 * wmax : L));
-  T.stencil = (P.stencil == 2 && proper) ? 2 : 1;
+  T.stencil = proper && P.stencil > 1 ? P.stencil : 1;
   const double wmin = fmin(T.wx, fmin(T.wy, T.wz));
-  T.r1_hmax = T.stencil == 2 ? 0.5 * wmin * (1.0 - 1e-9) : 1e300;
+  T.r1_hmax = T.stencil >= 2 ? 0.5 * wmin * (1.0 - 1e-9) : 1e300;
+  T.rw = 1.0 / (wmin * (1.0 - 1e-9));
   T.inv_wx = 1.0 / T.wx; T.inv_wy = 1.0 / T.wy; T.inv_wz = 1.0 / T.wz; T.inv_aw = 1.0 / T.aw;
 }
 
@@ -222,12 +223,14 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
   if (T.Cnx < 0 || T.Cny < 0 || T.Cnz < 0) return fail(c, DS_ERR_ARG, "box extent must be positive");
   if (T.ncells <= 0 || T.ncells > (1 << 28)) return fail(c, DS_ERR_ARG, "neighbour grid too large");
   if (T.n_idic <= 0 || T.n_idic > (1 << 28)) return fail(c, DS_ERR_ARG, "IDIC grid too large");
-  if (P.stencil != 0 && P.stencil != 1 && P.stencil != 2) return fail(c, DS_ERR_ARG, "stencil must be 1 or 2");
+  if (P.stencil < 0 || P.stencil > 4) return fail(c, DS_ERR_ARG, "stencil must be 1..4");
+  if (P.stencil > 2 && P.precision != DS_PRECISION_FP32)
+    return fail(c, DS_ERR_UNSUPPORTED, "stencils wider than 2 cells need the fp32 path");
   if (P.list_depth != 0 && P.list_depth != 32 && P.list_depth != 64)
     return fail(c, DS_ERR_ARG, "list_depth must be 0, 32 or 64");
   if (P.force_list < -1 || P.force_list > 4096) return fail(c, DS_ERR_ARG, "force_list must be -1, 0 or 1..4096");
-  if (P.stencil == 2 && !(P.mode & DS_MODE_GRID_PROPER))
-    return fail(c, DS_ERR_UNSUPPORTED, "stencil 2 needs the proper cell grid (DS_MODE_GRID_PROPER)");
+  if (P.stencil >= 2 && !(P.mode & DS_MODE_GRID_PROPER))
+    return fail(c, DS_ERR_UNSUPPORTED, "stencils of 2+ cells need the proper cell grid (DS_MODE_GRID_PROPER)");
   const int need = 2 * T.stencil + 1;  // a periodic axis must not alias its own stencil
   if ((P.mode & DS_MODE_PERIODIC_Y) && T.ny < need) return fail(c, DS_ERR_ARG, "too few cells across periodic y");
   if ((P.mode & DS_MODE_PERIODIC_Z) && T.nz < need) return fail(c, DS_ERR_ARG, "too few cells across periodic z");
@@ -292,7 +295,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   ds_launch_cell_start(skey, c->N, c->nkeys, c->cell_start, s);
   c->skey = skey;
   if (c->any_stencil2)
-    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->cbig, c->corx, c->d_nseg_key0, c->d_nseg_tube,
+    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->cwa, c->cwb, c->d_nseg_key0, c->d_nseg_tube,
                           c->d_nseg_species, c->nnseg, c->krad, s);
   c->parity ^= 1;
 }
@@ -384,13 +387,14 @@ ds_status finalize(ds_ctx *c) {
     if (P.mode & DS_MODE_GRID_PROPER) c->any_proper = true;
     if (P.mode & DS_MODE_DUST_RHO) c->any_dust_rho = true;
     if (P.precision == DS_PRECISION_FP32) c->any_fp32 = true;
-    if (T.stencil == 2) c->any_stencil2 = true;
+    if (T.stencil >= 2) c->any_stencil2 = true;
   }
   if (nkeys >= (1LL << 31) || nikeys >= (1LL << 31)) return fail(c, DS_ERR_ARG, "key space too large");
   for (const auto &T : c->tdesc)
     for (int s = 0; s < DS_MAXS; s++)
-      if (T.seg_end[s] - T.seg_begin[s] >= (1 << 25))
-        return fail(c, DS_ERR_UNSUPPORTED, "more than 2^25 particles in one species of a tube");
+      if (T.seg_end[s] - T.seg_begin[s] >= (T.precision == DS_PRECISION_FP32 ? (1 << 24) : (1 << 25)))
+        return fail(c, DS_ERR_UNSUPPORTED, "more particles in one species of a tube than a list entry holds "
+                                           "(2^24 on the fp32 path, 2^25 on the fp64 path)");
   // one kernel variant per batch: the mode bits that select templates must agree
   for (int t = 1; t < c->ntubes; t++) {
     const ds_params &P = c->params[t];
@@ -419,8 +423,8 @@ ds_status finalize(ds_ctx *c) {
   DA(c->slot_of_pid, N); DA(c->ind_of_pid, N); DA(c->idic_local, N);
   DA(c->cell_start, (size_t)nkeys + 1);
   DA(c->ncand, N); DA(c->nnb, N);
-  DA(c->cbig, (size_t)nkeys);
-  DA(c->corx, (size_t)nkeys);
+  DA(c->cwa, (size_t)nkeys);
+  DA(c->cwb, (size_t)nkeys);
   DA(c->krad, (size_t)nkeys);
   CK(cudaMemsetAsync(c->krad, 1, (size_t)nkeys, c->stream));
   DA(c->stage, N);
@@ -805,7 +809,7 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
   *count = 13 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
-           (c->any_stencil2 ? 3 : 0) + (c->nbl ? 1 : 0);
+           (c->any_stencil2 ? 4 : 0) + (c->nbl ? 1 : 0);
   return DS_OK;
 }
 

@@ -126,7 +126,9 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
       } else {
         ds_proper_cell(T, x, y, z, ix, iy, iz);
       }
-      p4.x = (float)(x - (T.ox + ix * T.wx));
+      // FP32 path: x relative to the x-block origin (row walks), y, z to the cell's
+      const int bx = FAST ? ((ix >> DS_XB_LOG) << DS_XB_LOG) : ix;
+      p4.x = (float)(x - (T.ox + bx * T.wx));
       p4.y = (float)(y - (T.oy + iy * T.wy));
       p4.z = (float)(z - (T.oz + iz * T.wz));
     } else {
@@ -541,43 +543,24 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
   }
 }
 
-// Stencil radius each cell's force sweep needs: 1 when no particle within R
-// cells (R = the tube's stencil) has h above half the cell width -- every
-// partner within the cut-off is then in the 27 inner cells -- else R.  Three
-// separable passes over the key space: a flag per cell (some h above the
-// limit), its OR over the x window, then over the y-z window (periodic axes
-// wrap).  Reference grids and the orphan buckets keep the tube's stencil.
-__global__ void k_cell_big(const TubeDesc *tubes, const int *cell_start, const int *nseg_key0,
-                           const int *nseg_tube, int nseg, int nkeys, const double *h, unsigned char *big) {
+// Stencil radius each cell's force sweep needs: the cells its particles'
+// partners (r < 2 max(h_i, h_j)) can lie in, i.e. ceil(2 H rw) with H the
+// largest h within the tube's stencil (ds_radius), so cells whose cut-offs are
+// short walk fewer cells.  Separable passes over the key space: h_max per cell,
+// its maximum over the x window, the y window, then the z window (periodic
+// axes wrap).  Reference grids and the orphan buckets keep the tube's stencil.
+__global__ void k_cell_hmax(const int *cell_start, int nkeys, const double *h, double *hmax) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
-  const double lim = tubes[nseg_tube[find_seg(nseg_key0, nseg, key)]].r1_hmax;
-  unsigned char b = 0;
-  for (int j = cell_start[key]; j < cell_start[key + 1]; j++) b |= (unsigned char)(h[j] > lim);
-  big[key] = b;
+  double m = 0.0;
+  for (int j = cell_start[key]; j < cell_start[key + 1]; j++) m = fmax(m, h[j]);
+  hmax[key] = m;
 }
 
-__global__ void k_cell_or_x(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
-                            const int *nseg_species, int nseg, int nkeys, const unsigned char *big,
-                            unsigned char *orx) {
-  const int key = blockIdx.x * blockDim.x + threadIdx.x;
-  if (key >= nkeys) return;
-  const int sg = find_seg(nseg_key0, nseg, key);
-  const TubeDesc &T = tubes[nseg_tube[sg]];
-  const int local = key - T.key_base[nseg_species[sg]];
-  if (T.stencil == 1 || local >= T.ncells || !(T.mode & M_GRID_PROPER)) {
-    orx[key] = big[key];
-    return;
-  }
-  const int ix = local % T.nx, R = T.stencil;
-  unsigned char b = 0;
-  for (int k = -R; k <= R; k++)
-    if (ix + k >= 0 && ix + k < T.nx) b |= big[key + k];
-  orx[key] = b;
-}
-
-__global__ void k_cell_radius(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
-                              const int *nseg_species, int nseg, int nkeys, const unsigned char *orx,
+// axis 0: x window, 1: y window, 2: z window (then the radius)
+template <int AXIS>
+__global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
+                              const int *nseg_species, int nseg, int nkeys, const double *in, double *out,
                               unsigned char *krad) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
@@ -585,23 +568,35 @@ __global__ void k_cell_radius(const TubeDesc *tubes, const int *nseg_key0, const
   const TubeDesc &T = tubes[nseg_tube[sg]];
   const int kb = T.key_base[nseg_species[sg]];
   const int local = key - kb;
-  if (T.stencil == 1) { krad[key] = 1; return; }
-  if (local >= T.ncells || !(T.mode & M_GRID_PROPER)) { krad[key] = (unsigned char)T.stencil; return; }
+  const bool whole = T.stencil == 1 || local >= T.ncells || !(T.mode & M_GRID_PROPER);
+  if (whole) {
+    if (AXIS == 2) krad[key] = (unsigned char)T.stencil;
+    else out[key] = in[key];
+    return;
+  }
   const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
   const int R = T.stencil;
-  unsigned char b = 0;
-  for (int l = -R; l <= R; l++) {
-    int cy = iy + l;
-    if (T.mode & M_PER_Y) cy = (cy + T.ny) % T.ny;
-    else if (cy < 0 || cy >= T.ny) continue;
-    for (int g = -R; g <= R; g++) {
-      int cz = iz + g;
+  double m = 0.0;
+  for (int d = -R; d <= R; d++) {
+    int c;
+    if (AXIS == 0) {
+      if (ix + d < 0 || ix + d >= T.nx) continue;
+      c = key + d;
+    } else if (AXIS == 1) {
+      int cy = iy + d;
+      if (T.mode & M_PER_Y) cy = (cy + T.ny) % T.ny;
+      else if (cy < 0 || cy >= T.ny) continue;
+      c = kb + ix + cy * T.sy + iz * T.sz;
+    } else {
+      int cz = iz + d;
       if (T.mode & M_PER_Z) cz = (cz + T.nz) % T.nz;
       else if (cz < 0 || cz >= T.nz) continue;
-      b |= orx[kb + ix + cy * T.sy + cz * T.sz];
+      c = kb + ix + iy * T.sy + cz * T.sz;
     }
+    m = fmax(m, in[c]);
   }
-  krad[key] = b ? (unsigned char)R : 1;
+  if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * m);
+  else out[key] = m;
 }
 
 __global__ void k_fill(double *a, int n, double v) {
@@ -695,11 +690,12 @@ void ds_launch_iota(int *a, int n, cudaStream_t s) {
   if (n > 0) k_iota<<<blocks_for(n, 256), 256, 0, s>>>(a, n);
 }
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, const double *h,
-                           unsigned char *big, unsigned char *orx, const int *nseg_key0, const int *nseg_tube,
+                           double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,
                            const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s) {
   if (nkeys <= 0) return;
   const int b = blocks_for(nkeys, 256);
-  k_cell_big<<<b, 256, 0, s>>>(tubes, cell_start, nseg_key0, nseg_tube, nseg, nkeys, h, big);
-  k_cell_or_x<<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, big, orx);
-  k_cell_radius<<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, orx, krad);
+  k_cell_hmax<<<b, 256, 0, s>>>(cell_start, nkeys, h, wa);
+  k_cell_window<0><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, wb, krad);
+  k_cell_window<1><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wb, wa, krad);
+  k_cell_window<2><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, nullptr, krad);
 }

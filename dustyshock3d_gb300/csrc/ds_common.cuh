@@ -53,9 +53,10 @@ struct TubeDesc {
   double fx, fy, fz;
   float pre_abs;   // absolute slack of the FP32 distance prefilter
   int cellrel;
-  int stencil;       // cells searched on each side (1: 27 cells, 2: 125 cells)
+  int stencil;       // cells searched on each side at most (FP64 path: 1 or 2; FP32 path: 1..4)
   int pad2;
   double r1_hmax;    // particles and cells with h <= r1_hmax need only the 27 inner cells
+  double rw;         // 1 / (min cell width (1 - 1e-9)): a cut-off c needs ceil(c rw) cells per side
   double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
   // segments
   int seg_begin[DS_MAXS], seg_end[DS_MAXS];
@@ -293,31 +294,6 @@ __device__ __forceinline__ void ds_shift32(const TubeDesc &T, const Stencil &S, 
   }
 }
 
-// FP32 shifts (k wx, l wy, g wz) of the 125 offset codes (k, l, g) in
-// [-2, 2]^3, formed as ds_shift32 forms them for cell-relative coordinates
-// (every tube on the FP32 path has them); one table per block, for the
-// tube of its chunk.
-#define DS_NOFS5 125
-__device__ __forceinline__ void ds_fill_shift_table(const TubeDesc &T, float4 *tab) {
-  const Shift32 f = ds_shift32_init(T);
-  for (int o5 = threadIdx.x; o5 < DS_NOFS5; o5 += blockDim.x) {
-    const int k = o5 / 25 - 2, l = (o5 / 5) % 5 - 2, g = o5 % 5 - 2;
-    tab[o5] = make_float4((float)k * f.wx, (float)l * f.wy, (float)g * f.wz, 0.0f);
-  }
-}
-
-// Shift of a list entry's cell minus the particle's own FP32 coordinates, as
-// ds_walk hands it to the screen (the same two roundings, so the pair work
-// sees the offsets the screen saw).
-__device__ __forceinline__ void ds_rel_shift32(const TubeDesc &T, const Stencil &S, const Shift32 &f,
-                                               const float4 &pi, int o5, float &ox, float &oy, float &oz) {
-  const int k = o5 / 25 - 2, l = (o5 / 5) % 5 - 2, g = o5 % 5 - 2;
-  ds_shift32(T, S, f, k, l, g, ox, oy, oz);
-  ox -= pi.x;
-  oy -= pi.y;
-  oz -= pi.z;
-}
-
 // Image shifts of the neighbour cell at offsets (l, g) from the own cell.
 __device__ __forceinline__ void ds_wrap_shift(const TubeDesc &T, const Stencil &S, int l, int g, double &shy,
                                               double &shz) {
@@ -411,6 +387,117 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
       for (int t = 0; t < DS_PIECE; t++) {
         const int j = j0 + p0 + t;
         pass[t] = (j < j1) && screen(j, sx, sy, sz);  // j1 - j0 <= len_w
+      }
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++)
+        if (pass[t]) {
+          lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t - sb);
+          n++;
+        }
+    }
+  }
+  flush();
+}
+
+// ---------------------------------------------------------------------------
+// FP32 path: x offsets relative to x-blocks of DS_XB cells, row walks
+// ---------------------------------------------------------------------------
+// On the FP32 path a particle's x is stored relative to the origin of its
+// x-block (DS_XB consecutive cells of its row; y and z stay relative to the
+// own cell).  The cells ix - r .. ix + r of one (y, z) row are consecutive
+// keys, so their particles are one slot range, and with block-relative x one
+// shift serves the whole range -- two ranges where the row crosses a block
+// edge.  Offset codes o = (db + 1) * 81 + (l + 4) * 9 + (g + 4) name the
+// neighbour block (db in -1..1) and row (l, g in -4..4); a list entry is
+// o << DS_OFS32_SHIFT | slot - segment start.
+#define DS_XB_LOG 4
+#define DS_XB (1 << DS_XB_LOG)
+#define DS_NOFS32 243
+#define DS_OFS32_SHIFT 24
+#define DS_SLOT32_MASK ((1u << DS_OFS32_SHIFT) - 1u)
+
+// cells each side a cut-off c needs (at least 1, at most the tube's stencil)
+__device__ __forceinline__ int ds_radius(const TubeDesc &T, double c) {
+  const int r = (int)ceil(c * T.rw);
+  return r < 1 ? 1 : (r > T.stencil ? T.stencil : r);
+}
+
+// FP32 shifts of the offset codes: (db DS_XB wx, l wy, g wz); one table per
+// block for the tube of its chunk
+__device__ __forceinline__ void ds_fill_shift_table32(const TubeDesc &T, float4 *tab) {
+  const float wx = (float)T.wx, wy = (float)T.wy, wz = (float)T.wz;
+  for (int o = threadIdx.x; o < DS_NOFS32; o += blockDim.x) {
+    const int db = o / 81 - 1, l = (o / 9) % 9 - 4, g = o % 9 - 4;
+    tab[o] = make_float4((float)(db * DS_XB) * wx, (float)l * wy, (float)g * wz, 0.0f);
+  }
+}
+
+// Warp-synchronous row walk with per-thread candidate lists (as ds_walk, over
+// half-rows instead of cells): rows (l, g) in [-r, r]^2, l outer; within a row
+// ascending slot.  screen(slot, ox, oy, oz) gets the range's shift minus the
+// particle's own FP32 coordinates; use(slot, code) runs over the survivors.
+template <int CAP, class Screen, class Use>
+__device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S, bool act, int r, int kb, int sb,
+                                             const int *cell_start, const float4 &pi, const float4 *shtab,
+                                             uint32_t *lst, Screen screen, Use use) {
+  const unsigned FULL = 0xffffffffu;
+  const int w = 2 * r + 1;
+  const int nq = act ? 2 * w * w : 0;
+  const int nq_w = __reduce_max_sync(FULL, nq);
+  const int bi = S.ix >> DS_XB_LOG;
+  const int cx0 = S.ix - r < 0 ? 0 : S.ix - r;
+  const int cx1 = S.ix + r > T.nx - 1 ? T.nx - 1 : S.ix + r;
+  const int bsplit = (cx1 >> DS_XB_LOG) << DS_XB_LOG;  // first cell of cx1's block
+  const bool split = bsplit > cx0;
+  int n = 0;
+  auto flush = [&]() {
+    const int nw = __reduce_max_sync(FULL, n);
+    for (int t = 0; t < nw; t++)
+      if (t < n) {
+        const uint32_t e = lst[t * DS_SWEEP_THREADS];
+        use(sb + (int)(e & DS_SLOT32_MASK), (int)(e >> DS_OFS32_SHIFT));
+      }
+    n = 0;
+  };
+  int l = -r, g = -r;
+  for (int q = 0; q < nq_w; q++) {
+    const int half = q & 1;
+    int j0 = 0, j1 = 0;
+    uint32_t code = 0;
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+    if (q < nq) {
+      int cy = S.iy + l, cz = S.iz + g;
+      bool ok = cx0 <= cx1;
+      if (T.mode & M_PER_Y) cy += cy < 0 ? T.ny : (cy >= T.ny ? -T.ny : 0);
+      else ok = ok && cy >= 0 && cy < T.ny;
+      if (T.mode & M_PER_Z) cz += cz < 0 ? T.nz : (cz >= T.nz ? -T.nz : 0);
+      else ok = ok && cz >= 0 && cz < T.nz;
+      const int a0 = half == 0 ? cx0 : bsplit;
+      const int a1 = half == 0 ? (split ? bsplit - 1 : cx1) : (split ? cx1 : bsplit - 1);
+      if (ok && a0 <= a1) {
+        const int base = kb + cy * T.sy + cz * T.sz;
+        j0 = cell_start[base + a0];
+        j1 = cell_start[base + a1 + 1];
+        const int o = ((a0 >> DS_XB_LOG) - bi + 1) * 81 + (l + 4) * 9 + (g + 4);
+        const float4 sh = shtab[o];
+        ox = sh.x - pi.x;
+        oy = sh.y - pi.y;
+        oz = sh.z - pi.z;
+        code = (uint32_t)o << DS_OFS32_SHIFT;
+      }
+      if (half == 1 && ++g > r) {
+        g = -r;
+        ++l;
+      }
+    }
+    const int len_w = __reduce_max_sync(FULL, j1 - j0);
+    for (int p0 = 0; p0 < len_w; p0 += DS_PIECE) {
+      if (__any_sync(FULL, n + DS_PIECE > CAP)) flush();
+      bool pass[DS_PIECE];
+#pragma unroll
+      for (int t = 0; t < DS_PIECE; t++) {
+        const int j = j0 + p0 + t;
+        pass[t] = (j < j1) && screen(j, ox, oy, oz);  // j1 - j0 <= len_w
       }
 #pragma unroll
       for (int t = 0; t < DS_PIECE; t++)

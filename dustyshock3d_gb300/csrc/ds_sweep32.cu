@@ -67,14 +67,14 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
 template <bool HPP, int WHAT, int CAP, bool LIST>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
-  __shared__ float4 shtab[DS_NOFS5];
+  __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const bool valid = i < ch.end && a.tstate[ch.tube].active;
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();  // the previous chunk's table is no longer read
-    ds_fill_shift_table(T, shtab);
+    ds_fill_shift_table32(T, shtab);
     __syncthreads();
     const int s = ch.species;
     const int ind = valid ? a.st.ind[i] : 1;
@@ -92,13 +92,13 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
     Stencil S{0, 0, 0, 0};
     if (upd) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
-    const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[a.skey[i]]) : (hd <= T.r1_hmax ? 1 : T.stencil);
+    const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[a.skey[i]]) : ds_radius(T, 2.0 * hd);
     const int sb = T.seg_begin[s];
     uint32_t *nl = LIST ? a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x : nullptr;
     int cnt = 0;
     Kahan sum;
-    ds_walk<CAP>(
-        T, S, upd, r, T.key_base[s], sb, a.cell_start, pi, lst + threadIdx.x,
+    ds_walk_rows<CAP>(
+        T, S, upd, r, T.key_base[s], sb, a.cell_start, pi, shtab, lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
           const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
           }
           if (LIST && r2 > 0.0f) {
             if (cnt < a.nbl_cap)
-              nl[(size_t)cnt * DS_SWEEP_THREADS] = ((uint32_t)o5 << DS_OFS_SHIFT) | (uint32_t)(j - sb);
+              nl[(size_t)cnt * DS_SWEEP_THREADS] = ((uint32_t)o5 << DS_OFS32_SHIFT) | (uint32_t)(j - sb);
             cnt++;
           }
         });
@@ -229,14 +229,14 @@ struct ForceSum {
 template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
-  __shared__ float4 shtab[DS_NOFS5];
+  __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     if (a.nbl && !a.nbl_walk[c]) continue;
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();
-    ds_fill_shift_table(T, shtab);
+    ds_fill_shift_table32(T, shtab);
     __syncthreads();
     const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int s = ch.species;
@@ -244,8 +244,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
     Stencil S{0, 0, 0, 0};
     if (act) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
     const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
-    ds_walk<CAP>(
-        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, lst + threadIdx.x,
+    ds_walk_rows<CAP>(
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, shtab, lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) { return F.screen(a.pos32[j], ox, oy, oz); },
         [&](int j, int o5) { F.pair(a, shtab[o5], j); });
     if (act) F.store(a, i);
@@ -260,14 +260,14 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
-  __shared__ float4 shtab[DS_NOFS5];
+  __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     if (a.nbl_walk[c]) continue;
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();
-    ds_fill_shift_table(T, shtab);
+    ds_fill_shift_table32(T, shtab);
     __syncthreads();
     const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int sb = T.seg_begin[ch.species];
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++)
         if (e + t < cnt) {
-          const int j = sb + (int)(ent[t] & DS_SLOT_MASK);
+          const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
           pj[t] = a.pos32[j];
           vmj[t] = a.vm32[j];
           hyj[t] = a.hyd32[j];
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
       }
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++)
-        if (e + t < cnt) F.pair(shtab[ent[t] >> DS_OFS_SHIFT], pj[t], vmj[t], hyj[t]);
+        if (e + t < cnt) F.pair(shtab[ent[t] >> DS_OFS32_SHIFT], pj[t], vmj[t], hyj[t]);
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++) ent[t] = nxt[t];
     }

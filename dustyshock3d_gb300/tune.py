@@ -2,9 +2,10 @@
 
 Knobs (all results stay within the FP32 path's tolerance; none changes the
 physics):
-  * cell size and stencil: cells of width ~h_max searched 2 cells on each side
-    (a particle whose cut-off fits walks only the 27 inner cells), or cells of
-    width ~2 h_max searched 1 cell on each side; plus the cell-width margin;
+  * cell size and stencil: cells of width ~2 h_max searched 1 cell on each
+    side, ~h_max searched up to 2, ~2/3 h_max up to 3 or ~h_max / 2 up to 4
+    (each cell walks only as many as its particles' cut-offs reach; smaller
+    cells screen fewer candidates per pair, in more rows);
   * list depth: candidate-list entries per thread (32 or 64), i.e. how many
     screened neighbours a thread stages before the pair work runs.
 
@@ -24,8 +25,9 @@ from .species import Species
 CANDIDATES = [
     (2, 1.001, 32),
     (2, 1.001, 64),
-    (2, 1.10, 32),
     (1, 2.002, 32),
+    (3, 0.6673, 32),
+    (4, 0.5005, 32),
 ]
 
 

@@ -83,10 +83,11 @@ typedef struct ds_params {
   int n_dust;                /* dust species, 1..DS_MAX_DUST (reference: 2)      */
   int mode;                  /* DS_MODE_* bits                                   */
   int precision;             /* DS_PRECISION_*                                   */
-  int stencil;               /* cells searched on each side: 0 or 1 -> 27 cells of width
-                                >= 2h (the reference); 2 -> 125 cells of width >= h_max
-                                (DS_MODE_GRID_PROPER), each particle walking only the 27
-                                inner cells when its cut-off fits them                 */
+  int stencil;               /* cells searched on each side at most: 0 or 1 -> 27 cells of
+                                width >= 2h (the reference); 2 -> up to 125 cells of width
+                                >= h_max (DS_MODE_GRID_PROPER), each particle walking only
+                                the cells its cut-off reaches; 3 or 4 (fp32 path only) ->
+                                smaller cells, up to 9 x 9 rows of 9 cells             */
   double cell_w;             /* neighbour cell width; 0 -> 2h (kernel.cu:1773)   */
   double idic_w;             /* IDIC cell width; 0 -> Coeff_h_dust_cell*h (kernel.cu:1577) */
   double cfl;                /* CFL number (DS_MODE_CFL)                          */

@@ -136,13 +136,18 @@ def test_baseline_lists_and_counts_bitexact():
             assert (dbg["ncand"] == nc).all() and (dbg["nnb"] == nn).all()
 
 
-def test_fp32_path_against_fp64_oracle():
-    """FP32 sweeps (Kahan sums, cell-relative FP32 positions) vs the FP64 oracle:
-    relative L1 of gas density <= 1e-5 after 10 steps, velocities <= 1e-4 of the
-    velocity scale."""
+@pytest.mark.parametrize("stencil,cell_factor", [(2, 1.001), (3, 0.6673), (4, 0.5005)])
+def test_fp32_path_against_fp64_oracle(stencil, cell_factor):
+    """FP32 sweeps (Kahan sums, FP32 positions relative to cell / x-block
+    origins, row walks) vs the FP64 oracle on its own grid: relative L1 of gas
+    density <= 1e-5 after 10 steps, velocities <= 1e-4 of the velocity scale.
+    Smaller cells with wider stencils (cells of h_max / 2, up to 9 cells per
+    side for the right state's longer cut-off) give the same physics."""
     P, sp = small_tube()
     P32 = P.copy()
     P32.precision = "fp32"
+    P32.stencil = stencil
+    P32.cell_w = cell_factor * P.h
     gpu, _ = run_gpu(P32, sp, 10)
     O = OracleState(P, sp).step(10)
     g, o = gpu[0], O.species[0]
@@ -153,8 +158,8 @@ def test_fp32_path_against_fp64_oracle():
     assert np.abs(gpu[1].vx - O.species[1].vx).mean() / vscale < 1e-4
 
 
-@pytest.mark.parametrize("cap", [0, 100, 8])
-def test_fp32_force_lists_equal_walk(cap):
+@pytest.mark.parametrize("cap,stencil", [(0, 2), (100, 2), (8, 2), (0, 4), (100, 4)])
+def test_fp32_force_lists_equal_walk(cap, stencil):
     """The FP32 force sweep over the neighbours recorded by the density sweep
     equals the force sweep's own cell walk bit for bit: every chunk listed
     (0 -> 256 entries), listed and walked chunks mixed (100: interior gas has
@@ -162,6 +167,8 @@ def test_fp32_force_lists_equal_walk(cap):
     walked (8)."""
     P, sp = small_tube()
     P.precision = "fp32"
+    if stencil == 4:
+        P.stencil, P.cell_w = 4, 0.5005 * P.h
     Pw = P.copy()
     Pw.force_list = -1
     walk, tw = run_gpu(Pw, sp, 8)
