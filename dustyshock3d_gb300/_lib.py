@@ -68,6 +68,7 @@ SIGNATURES = {
     "ds_step_timed": ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
                       ctypes.c_int),
     "ds_kernels_per_step": ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "ds_dust_density": ([_VP], ctypes.c_int),
     "ds_memory_bytes": ([_VP, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "ds_last_error": ([_VP, _IP, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
     "ds_cell_lists_noalloc": ([ctypes.POINTER(DsParams), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,

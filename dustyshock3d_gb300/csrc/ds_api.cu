@@ -270,6 +270,7 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.gas_ind_pid = c->ind_of_pid;
   a.tstate_rw = c->d_tstate;
   a.flags = c->d_flags;
+  a.all_tubes = 0;
   a.nbl = nullptr;
   a.nbl_cnt = nullptr;
   a.nbl_walk = nullptr;
@@ -800,6 +801,22 @@ ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms)
   if (phase_ms)
     for (int p = 0; p < DS_NPHASE; p++) phase_ms[p] = acc[p];
   return check_flags(c);
+}
+
+ds_status ds_dust_density(ds_ctx *c) {
+  if (!c) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  CK(cudaSetDevice(c->device));
+  if (c->ch_dust.empty()) return DS_OK;
+  enqueue_sort(c);  // cells for the current positions (caller-index order on the FP64 path)
+  SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
+  ad.all_tubes = 1;
+  if (c->any_fp32) ds_launch_density32(ad, c->any_hpp, 1, c->params[0].list_depth, c->stream);
+  else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
 }
 
 ds_status ds_kernels_per_step(ds_ctx *c, int *count) {

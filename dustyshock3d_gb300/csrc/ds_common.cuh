@@ -540,6 +540,7 @@ struct SweepArgs {
   const int *gas_ind_pid;      // gas Ind by pid (index-coupled dust rho zeroing)
   TubeState *tstate_rw;
   int *flags;
+  int all_tubes;               // density on demand: tubes past their end time too
   // FP32 force neighbour lists (recorded by the gas density sweep): entry e of
   // the particle in lane t of gas chunk c at nbl[(c * nbl_cap + e) * 128 + t]
   uint32_t *nbl;               // nullptr: the force sweep walks the cells

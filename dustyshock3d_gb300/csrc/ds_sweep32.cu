@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
-    const bool valid = i < ch.end && a.tstate[ch.tube].active;
+    const bool valid = i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();  // the previous chunk's table is no longer read
     ds_fill_shift_table32(T, shtab);

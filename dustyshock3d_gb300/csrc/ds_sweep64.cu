@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
-    const bool valid = i < ch.end && a.tstate[ch.tube].active;
+    const bool valid = i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
     const TubeDesc &T = a.tubes[ch.tube];
     const int s = ch.species;
     const int ind = valid ? a.st.ind[i] : 1;

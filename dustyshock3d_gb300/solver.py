@@ -151,6 +151,11 @@ class Solver:
         _lib.check(self.L, self.ctx, self.L.ds_conservation(self.ctx, tube, _dp(out)), "ds_conservation")
         return out
 
+    def dust_density(self):
+        """Dust self-density of every tube at the current positions (the
+        reference's output-only sweep, kernel.cu:2029-2043), on demand."""
+        _lib.check(self.L, self.ctx, self.L.ds_dust_density(self.ctx), "ds_dust_density")
+
     def kernels_per_step(self):
         k = ctypes.c_int(0)
         _lib.check(self.L, self.ctx, self.L.ds_kernels_per_step(self.ctx, ctypes.byref(k)), "ds_kernels_per_step")

@@ -196,6 +196,13 @@ ds_status ds_debug_idic(ds_ctx *c, int tube, int species, int *count, double *ce
  * internal energy sum m e, out[5] kinetic energy (all species). */
 ds_status ds_conservation(ds_ctx *c, int tube, double *out6);
 
+/* Dust self-density of every tube at the current positions (kernel.cu:2029-2043),
+ * computed on demand: the reference computes it every step but only its snapshot
+ * writer reads it (kernel.cu:2547-2562), so a host that writes snapshots calls
+ * this before ds_get_dust / ds_download_dust at output times instead of paying
+ * for it every step (DS_MODE_DUST_RHO).  Same sums as the per-step sweep. */
+ds_status ds_dust_density(ds_ctx *c);
+
 /* Runs nsteps steps back to back (the graph's kernels, launched one by one)
  * with CUDA events between phases on the context's stream; returns the total
  * device time and the per-phase sums in milliseconds: [0] keys, sort, reorder,

@@ -7,6 +7,8 @@ Bit-exactness claims:
     and summation order, no FMA contraction) -- floats compared with ==;
   * the FP32 path is compared with a stated tolerance.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -177,6 +179,33 @@ def test_fp32_force_lists_equal_walk(cap, stencil):
     listed, tl = run_gpu(Pl, sp, 8)
     assert tw == tl
     compare_exact(listed, walk, f"force_list={cap}")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_dust_density_on_demand(precision):
+    """ds_dust_density after N steps without the per-step dust sweep equals the
+    oracle's dust self-density at the same positions (the oracle computes it
+    at the start of its next step, from the GPU's state): bit for bit on the
+    FP64 path, relative L1 <= 1e-6 on the FP32 path."""
+    P, sp = small_tube()
+    P.precision = precision
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(5)
+        S.dust_density()
+        g = S.get_species(0, 0)
+        d = S.get_species(0, 1)
+    g.m, g.h = sp[0].m, sp[0].h
+    d.m, d.h = sp[1].m, sp[1].h
+    Q = P.copy()
+    Q.precision = "fp64"
+    Q.mode = dataclasses.replace(P.mode, dust_rho=True)
+    O = OracleState(Q, [g, d]).step(1)
+    ref = O.species[1].rho
+    if precision == "fp64":
+        assert_equal_nan(d.rho, ref, "dust rho")
+    else:
+        assert np.abs(d.rho - ref).sum() / np.abs(ref).sum() < 1e-6
 
 
 def test_batched_tubes_equal_single_runs():
