@@ -60,6 +60,7 @@ struct ds_ctx {
   // sizes
   int N = 0;
   int nkeys = 0, key_bits = 0, nikeys = 0, ikey_bits = 0, ncell_total = 0, nseg = 0, nnseg = 0;
+  int xl = 0;  // FP32 path: sub-cell x bits below the cell in the sort keys
   std::vector<TubeDesc> tdesc;
   std::vector<Chunk> ch_all, ch_gas, ch_dust;
   // device
@@ -101,6 +102,10 @@ struct ds_ctx {
 };
 
 static_assert(DS_CHUNK == DS_SWEEP_THREADS, "one sweep thread per particle of a chunk");
+
+#ifndef DS_XL_MAX
+#define DS_XL_MAX 4  // x bins per cell on the FP32 path: at most 2^DS_XL_MAX (measured: 16 bins beat 8, 32, 64)
+#endif
 
 namespace {
 
@@ -286,17 +291,18 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   DevState src = c->buf[c->parity].view();
   DevState dst = c->buf[c->parity ^ 1].view();
   const bool fast = c->any_fp32 && !exact_order;
+  const int xl = fast ? c->xl : 0;  // fast keys carry the x bin below the cell
   ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s);
   bool alt = false;
-  ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits, c->rs_scratch, s, &alt);
+  ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt);
   const uint32_t *skey = alt ? c->kalt : c->kin;
   const uint32_t *sval = alt ? c->valt : c->vin;
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
                     c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, fast, s);
-  ds_launch_cell_start(skey, c->N, c->nkeys, c->cell_start, s);
+  ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s);
   c->skey = skey;
   if (c->any_stencil2)
-    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, dst.h, c->cwa, c->cwb, c->d_nseg_key0, c->d_nseg_tube,
+    ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, xl, dst.h, c->cwa, c->cwb, c->d_nseg_key0, c->d_nseg_tube,
                           c->d_nseg_species, c->nnseg, c->krad, s);
   c->parity ^= 1;
 }
@@ -406,6 +412,14 @@ ds_status finalize(ds_ctx *c) {
   c->N = N;
   c->nkeys = (int)nkeys;
   c->key_bits = bits_for(nkeys);
+  // FP32 path: up to 2^DS_XL_MAX x bins per cell, as long as the start table stays
+  // within ~8 entries per particle and the keys within 31 bits
+  c->xl = 0;
+  if (c->any_fp32 && c->any_proper) {
+    c->xl = DS_XL_MAX;
+    while (c->xl > 0 && ((nkeys << c->xl) > 8LL * N + 4096 || c->key_bits + c->xl > 31)) c->xl--;
+  }
+  for (auto &T : c->tdesc) T.xl = c->xl;
   c->nikeys = (int)nikeys;
   c->ikey_bits = bits_for(nikeys);
   c->ncell_total = (int)ncell;
@@ -422,7 +436,7 @@ ds_status finalize(ds_ctx *c) {
   DA(c->ikin, N); DA(c->ivin, N); DA(c->ikalt, N); DA(c->ivalt, N);
   DA(c->rs_scratch, ds_radix_scratch_words(N));
   DA(c->slot_of_pid, N); DA(c->ind_of_pid, N); DA(c->idic_local, N);
-  DA(c->cell_start, (size_t)nkeys + 1);
+  DA(c->cell_start, ((size_t)nkeys << c->xl) + 1);
   DA(c->ncand, N); DA(c->nnb, N);
   DA(c->cwa, (size_t)nkeys);
   DA(c->cwb, (size_t)nkeys);
@@ -825,7 +839,7 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   if (st != DS_OK) return st;
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
-  *count = 13 + 3 * (ds_radix_passes(c->key_bits) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
+  *count = 13 + 3 * (ds_radix_passes(c->key_bits + c->xl) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
            (c->any_stencil2 ? 4 : 0) + (c->nbl ? 1 : 0);
   return DS_OK;
 }

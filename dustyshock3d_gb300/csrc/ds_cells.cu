@@ -65,11 +65,20 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
     if (i >= ch.end) continue;
     const TubeDesc &T = tubes[ch.tube];
     int local;
+    uint32_t bin = 0;
     if (FAST && (T.mode & M_GRID_PROPER)) {
       int ix, iy, iz;
       ds_fast_proper_cell(T, st.x[i], st.y[i], st.z[i], ix, iy, iz);
       const bool in = ix >= 0 && ix < T.nx && iy >= 0 && iy < T.ny && iz >= 0 && iz < T.nz;
       local = in ? ix + iy * T.sy + iz * T.sz : T.ncells + 1;
+      // FP32 path: the particle's x within its cell in 2^xl bins, below the
+      // cell in the key, so that each cell -- and so each row of cells -- is
+      // sorted by x
+      if (in) {
+        const double fx = (st.x[i] - T.ox) * T.inv_wx - (double)ix;
+        const int b = (int)(fx * (double)(1 << T.xl));
+        bin = (uint32_t)(b < 0 ? 0 : (b >= (1 << T.xl) ? (1 << T.xl) - 1 : b));
+      }
     } else {
       const int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
       if (!(T.mode & M_GRID_PROPER))
@@ -78,7 +87,8 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
         local = key >= 0 ? key : T.ncells + 1;
     }
     const int dst = FAST ? i : T.seg_begin[ch.species] + st.pid[i];
-    kin[dst] = (uint32_t)(T.key_base[ch.species] + local);
+    kin[dst] = FAST ? ((uint32_t)(T.key_base[ch.species] + local) << T.xl) | bin
+                    : (uint32_t)(T.key_base[ch.species] + local);
     vin[dst] = (uint32_t)i;
   }
 }
@@ -115,7 +125,7 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     // grid), or from the tube's reference point (reference grid)
     float4 p4;
     if (T.cellrel) {
-      const int local = (int)skey[q] - T.key_base[ch.species];
+      const int local = (int)(skey[q] >> (FAST ? T.xl : 0)) - T.key_base[ch.species];
       int ix, iy, iz;
       if (local < T.ncells) {
         ix = local % T.nx;
@@ -549,11 +559,11 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
 // short walk fewer cells.  Separable passes over the key space: h_max per cell,
 // its maximum over the x window, the y window, then the z window (periodic
 // axes wrap).  Reference grids and the orphan buckets keep the tube's stencil.
-__global__ void k_cell_hmax(const int *cell_start, int nkeys, const double *h, double *hmax) {
+__global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const double *h, double *hmax) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
   double m = 0.0;
-  for (int j = cell_start[key]; j < cell_start[key + 1]; j++) m = fmax(m, h[j]);
+  for (int j = cell_start[key << xl]; j < cell_start[(key + 1) << xl]; j++) m = fmax(m, h[j]);
   hmax[key] = m;
 }
 
@@ -689,12 +699,12 @@ void ds_launch_fill(double *a, int n, double v, cudaStream_t s) {
 void ds_launch_iota(int *a, int n, cudaStream_t s) {
   if (n > 0) k_iota<<<blocks_for(n, 256), 256, 0, s>>>(a, n);
 }
-void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, const double *h,
+void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, int xl, const double *h,
                            double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,
                            const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s) {
   if (nkeys <= 0) return;
   const int b = blocks_for(nkeys, 256);
-  k_cell_hmax<<<b, 256, 0, s>>>(cell_start, nkeys, h, wa);
+  k_cell_hmax<<<b, 256, 0, s>>>(cell_start, nkeys, xl, h, wa);
   k_cell_window<0><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, wb, krad);
   k_cell_window<1><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wb, wa, krad);
   k_cell_window<2><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, nullptr, krad);

@@ -54,7 +54,7 @@ struct TubeDesc {
   float pre_abs;   // absolute slack of the FP32 distance prefilter
   int cellrel;
   int stencil;       // cells searched on each side at most (FP64 path: 1 or 2; FP32 path: 1..4)
-  int pad2;
+  int xl;            // FP32 path: sub-cell x bits of the sort keys (key = cell << xl | x bin)
   double r1_hmax;    // particles and cells with h <= r1_hmax need only the 27 inner cells
   double rw;         // 1 / (min cell width (1 - 1e-9)): a cut-off c needs ceil(c rw) cells per side
   double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
@@ -437,21 +437,33 @@ __device__ __forceinline__ void ds_fill_shift_table32(const TubeDesc &T, float4 
 
 // Warp-synchronous row walk with per-thread candidate lists (as ds_walk, over
 // half-rows instead of cells): rows (l, g) in [-r, r]^2, l outer; within a row
-// ascending slot.  screen(slot, ox, oy, oz) gets the range's shift minus the
-// particle's own FP32 coordinates; use(slot, code) runs over the survivors.
+// ascending slot.  The sort keys carry T.xl bits of x within the cell, so a
+// row's slots are sorted by x and cell_start (indexed by cell << xl | bin)
+// bounds the lane's x window [x - cutx, x + cutx] (one bin of slack each
+// side) instead of the whole row: every lane's window has the same length.
+// screen(slot, ox, oy, oz) gets the range's shift minus the particle's own
+// FP32 coordinates; use(slot, code) runs over the survivors.
 template <int CAP, class Screen, class Use>
 __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S, bool act, int r, int kb, int sb,
-                                             const int *cell_start, const float4 &pi, const float4 *shtab,
-                                             uint32_t *lst, Screen screen, Use use) {
+                                             const int *cell_start, const float4 &pi, float cutx,
+                                             const float4 *shtab, uint32_t *lst, Screen screen, Use use) {
   const unsigned FULL = 0xffffffffu;
   const int w = 2 * r + 1;
   const int nq = act ? 2 * w * w : 0;
   const int nq_w = __reduce_max_sync(FULL, nq);
+  const int xl = T.xl;
   const int bi = S.ix >> DS_XB_LOG;
   const int cx0 = S.ix - r < 0 ? 0 : S.ix - r;
   const int cx1 = S.ix + r > T.nx - 1 ? T.nx - 1 : S.ix + r;
-  const int bsplit = (cx1 >> DS_XB_LOG) << DS_XB_LOG;  // first cell of cx1's block
-  const bool split = bsplit > cx0;
+  // the window in fine x indices (cell << xl | bin), clipped to the row
+  const float sc = (float)(1 << xl) * (float)T.inv_wx;
+  const int fb = (bi * DS_XB) << xl;  // fine index of the own block's origin
+  int f_lo = fb + (int)floorf((pi.x - cutx) * sc) - 1;
+  int f_hi = fb + (int)floorf((pi.x + cutx) * sc) + 1;
+  f_lo = f_lo < (cx0 << xl) ? (cx0 << xl) : f_lo;
+  f_hi = f_hi > ((cx1 + 1) << xl) - 1 ? ((cx1 + 1) << xl) - 1 : f_hi;
+  const int bsplit = (f_hi >> (xl + DS_XB_LOG)) << (xl + DS_XB_LOG);  // first fine index of f_hi's block
+  const bool split = bsplit > f_lo;
   int n = 0;
   auto flush = [&]() {
     const int nw = __reduce_max_sync(FULL, n);
@@ -470,18 +482,18 @@ __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S
     float ox = 0.0f, oy = 0.0f, oz = 0.0f;
     if (q < nq) {
       int cy = S.iy + l, cz = S.iz + g;
-      bool ok = cx0 <= cx1;
+      bool ok = f_lo <= f_hi;
       if (T.mode & M_PER_Y) cy += cy < 0 ? T.ny : (cy >= T.ny ? -T.ny : 0);
       else ok = ok && cy >= 0 && cy < T.ny;
       if (T.mode & M_PER_Z) cz += cz < 0 ? T.nz : (cz >= T.nz ? -T.nz : 0);
       else ok = ok && cz >= 0 && cz < T.nz;
-      const int a0 = half == 0 ? cx0 : bsplit;
-      const int a1 = half == 0 ? (split ? bsplit - 1 : cx1) : (split ? cx1 : bsplit - 1);
+      const int a0 = half == 0 ? f_lo : bsplit;
+      const int a1 = half == 0 ? (split ? bsplit - 1 : f_hi) : (split ? f_hi : bsplit - 1);
       if (ok && a0 <= a1) {
-        const int base = kb + cy * T.sy + cz * T.sz;
+        const int base = (kb + cy * T.sy + cz * T.sz) << xl;
         j0 = cell_start[base + a0];
         j1 = cell_start[base + a1 + 1];
-        const int o = ((a0 >> DS_XB_LOG) - bi + 1) * 81 + (l + 4) * 9 + (g + 4);
+        const int o = ((a0 >> (xl + DS_XB_LOG)) - bi + 1) * 81 + (l + 4) * 9 + (g + 4);
         const float4 sh = shtab[o];
         ox = sh.x - pi.x;
         oy = sh.y - pi.y;

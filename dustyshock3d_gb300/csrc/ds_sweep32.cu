@@ -91,14 +91,17 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
     const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
     Stencil S{0, 0, 0, 0};
-    if (upd) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
-    const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[a.skey[i]]) : ds_radius(T, 2.0 * hd);
+    const int own = upd ? (int)(a.skey[i] >> T.xl) : 0;  // own cell key
+    if (upd) ds_stencil_from_key(T, own - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
+    const int r = LIST ? ((T.stencil == 1 || !upd) ? 1 : (int)a.krad[own]) : ds_radius(T, 2.0 * hd);
+    // x reach of the partners: r cells (every partner lies within them) or 2 h
+    const float cutx = LIST ? (float)r * (float)T.wx : 2.0f * hf;
     const int sb = T.seg_begin[s];
     uint32_t *nl = LIST ? a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x : nullptr;
     int cnt = 0;
     Kahan sum;
     ds_walk_rows<CAP>(
-        T, S, upd, r, T.key_base[s], sb, a.cell_start, pi, shtab, lst + threadIdx.x,
+        T, S, upd, r, T.key_base[s], sb, a.cell_start, pi, cutx, shtab, lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) {
           const float4 pj = a.pos32[j];
           const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
@@ -242,10 +245,12 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
     const int s = ch.species;
     ForceSum<HPP> F(a, T, i, act);
     Stencil S{0, 0, 0, 0};
-    if (act) ds_stencil_from_key(T, (int)a.skey[i] - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
-    const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[a.skey[i]];
+    const int own = act ? (int)(a.skey[i] >> T.xl) : 0;  // own cell key
+    if (act) ds_stencil_from_key(T, own - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
+    const int r = (T.stencil == 1 || !act) ? 1 : (int)a.krad[own];
     ds_walk_rows<CAP>(
-        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, shtab, lst + threadIdx.x,
+        T, S, act, r, T.key_base[s], T.seg_begin[s], a.cell_start, F.pi, (float)r * (float)T.wx, shtab,
+        lst + threadIdx.x,
         [&](int j, float ox, float oy, float oz) { return F.screen(a.pos32[j], ox, oy, oz); },
         [&](int j, int o5) { F.pair(a, shtab[o5], j); });
     if (act) F.store(a, i);
