@@ -185,6 +185,12 @@ class OracleState:
         Tm = ctypes.c_double(self.Tm)
         dt = ctypes.c_double(0.0)
         for _ in range(n):
+            # the reference's loop runs while Tm < T_end (kernel.cu:1929, 2566): a
+            # step after the end time does nothing (and reports dt = 0, as the
+            # GPU does)
+            if Tm.value >= self.P.T_end:
+                dt.value = 0.0
+                continue
             st = L.orc_step(ctypes.byref(self.P), self._arr, ctypes.byref(Tm), ctypes.byref(dt))
             if st < 0:
                 raise ValueError("oracle: a periodic axis has fewer cells than its stencil needs")
