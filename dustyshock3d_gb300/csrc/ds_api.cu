@@ -448,7 +448,7 @@ ds_status finalize(ds_ctx *c) {
     c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : 256;
     DA(c->nbl, c->ch_gas.size() * (size_t)c->nbl_cap * DS_CHUNK);
     DA(c->nbl_cnt, N);
-    DA(c->nbl_walk, c->ch_gas.size());
+    DA(c->nbl_walk, c->ch_gas.size() * (DS_SWEEP_THREADS / 32));
   }
   DA(c->d_cons, 8);
   DA(c->d_flags, 1);

@@ -557,6 +557,6 @@ struct SweepArgs {
   // the particle in lane t of gas chunk c at nbl[(c * nbl_cap + e) * 128 + t]
   uint32_t *nbl;               // nullptr: the force sweep walks the cells
   int *nbl_cnt;                // entries per slot
-  unsigned char *nbl_walk;     // per gas chunk: 1 when a particle overflowed (that chunk walks)
+  unsigned char *nbl_walk;     // per warp of each gas chunk: 1 when a particle overflowed (that warp walks)
   int nbl_cap;
 };

@@ -59,8 +59,8 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
 // 2 max(h_i, h_j) (a superset of its own 2 h_i: the density adds only pairs
 // within 2 h_i, so its sum is unchanged), and writes each pair with r > 0 --
 // exactly the pairs the force sweep's own walk would accept, in its visiting
-// order.  A chunk with a particle beyond nbl_cap entries is flagged; the force
-// sweep walks that chunk.
+// order.  A warp with a particle beyond nbl_cap entries is flagged (one flag
+// per warp, no block barrier); the force sweep walks that warp's particles.
 #ifndef DS_DENS_LIST_MINB
 #define DS_DENS_LIST_MINB 6  // blocks per SM the list-recording density sweep is built for
 #endif
@@ -126,8 +126,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
           }
         });
     if (LIST) {
-      const int over = __syncthreads_or(cnt > a.nbl_cap);
-      if (threadIdx.x == 0) a.nbl_walk[c] = (unsigned char)(over != 0);
+      const unsigned over = __ballot_sync(0xffffffffu, cnt > a.nbl_cap);
+      if ((threadIdx.x & 31) == 0) a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)] = over != 0u;
       if (i < ch.end) a.nbl_cnt[i] = cnt;
     }
     if (!valid) continue;
@@ -227,21 +227,27 @@ struct ForceSum {
   }
 };
 
+// The 4 warp flags of a chunk as one word (nbl_walk is 4-byte aligned per chunk).
+__device__ __forceinline__ uint32_t chunk_walk_flags(const SweepArgs &a, int c) {
+  return *reinterpret_cast<const uint32_t *>(a.nbl_walk + (size_t)c * (DS_SWEEP_THREADS / 32));
+}
+
 // Force sweep by walking the stencil.  With recorded lists it runs only the
-// chunks flagged as overflowed.
+// warps flagged as overflowed.
 template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
-    if (a.nbl && !a.nbl_walk[c]) continue;
+    if (a.nbl && chunk_walk_flags(a, c) == 0u) continue;  // uniform per block
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();
     ds_fill_shift_table32(T, shtab);
     __syncthreads();
-    const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
+    const bool mine = !a.nbl || a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)];
+    const bool act = mine && i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int s = ch.species;
     ForceSum<HPP> F(a, T, i, act);
     Stencil S{0, 0, 0, 0};
@@ -267,14 +273,15 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
-    if (a.nbl_walk[c]) continue;
+    if (chunk_walk_flags(a, c) == 0x01010101u) continue;  // every warp walks instead; uniform per block
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();
     ds_fill_shift_table32(T, shtab);
     __syncthreads();
-    const bool act = i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
+    const bool listed = !a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)];
+    const bool act = listed && i < ch.end && a.tstate[ch.tube].active && a.st.ind[i] == 0;
     const int sb = T.seg_begin[ch.species];
     ForceSum<HPP> F(a, T, i, act);
     const int cnt = act ? a.nbl_cnt[i] : 0;
