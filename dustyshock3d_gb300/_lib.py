@@ -69,6 +69,9 @@ SIGNATURES = {
                       ctypes.c_int),
     "ds_kernels_per_step": ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "ds_dust_density": ([_VP], ctypes.c_int),
+    "ds_save_tube": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+    "ds_checkpoint_params": ([ctypes.c_char_p, ctypes.POINTER(DsParams)], ctypes.c_int),
+    "ds_load_tube": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
     "ds_memory_bytes": ([_VP, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "ds_last_error": ([_VP, _IP, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
     "ds_cell_lists_noalloc": ([ctypes.POINTER(DsParams), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
@@ -128,6 +131,29 @@ def params_to_c(P: Params) -> DsParams:
         c.t_stop_const[k] = float(P.t_stop_const[k]) if k < len(P.t_stop_const) else 0.0
         c.eps_empty[k] = float(P.eps_empty[k]) if k < len(P.eps_empty) else 0.0
     return c
+
+
+def params_from_c(c: DsParams) -> Params:
+    """Inverse of params_to_c."""
+    P = Params()
+    for f in ("X_min", "X_max", "Y_min", "Y_max", "Z_min", "Z_max", "Particle_on_length", "h",
+              "Coeff_h_dust_cell", "tau", "T_end", "T_out", "alpha", "beta", "eps", "Gam_g",
+              "Speed_of_sound_gas", "cell_w", "idic_w", "cfl", "t_empty"):
+        setattr(P, f, float(getattr(c, f)))
+    P.Type_of_state = int(c.Type_of_state)
+    P.Maximum_particle = int(c.Maximum_particle)
+    P.n_dust = int(c.n_dust)
+    for name, bit in MODE_BITS.items():
+        setattr(P.mode, name, bool(c.mode & bit))
+    P.precision = "fp32" if c.precision == 1 else "fp64"
+    P.stencil = int(c.stencil)
+    P.list_depth = int(c.list_depth)
+    P.force_list = int(c.force_list)
+    P.mass_ratio = [float(c.mass_ratio[k]) for k in range(P.n_dust)]
+    P.R_dust = [float(c.R_dust[k]) for k in range(P.n_dust)]
+    P.t_stop_const = [float(c.t_stop_const[k]) for k in range(P.n_dust)]
+    P.eps_empty = [float(c.eps_empty[k]) for k in range(P.n_dust)]
+    return P
 
 
 def check(L, ctx, status: int, what: str):

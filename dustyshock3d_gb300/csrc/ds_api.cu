@@ -7,6 +7,7 @@
 // stream with no host work and no copies; the sequence is captured once into a
 // CUDA graph per buffer parity and replayed.
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -55,6 +56,7 @@ struct ds_ctx {
   std::vector<ds_params> params;
   std::vector<std::vector<HostSpecies>> host;  // [tube][species]
   std::vector<std::pair<ds_ctx *, int>> dev_src;  // per tube: resident tube to copy from (ds_copy_tube)
+  std::vector<std::pair<bool, std::pair<double, long long>>> clock_set;  // per tube: clock to start from
   bool finalized = false;
   std::string msg;
   // sizes
@@ -514,6 +516,15 @@ ds_status finalize(ds_ctx *c) {
     }
     CK(cudaMemcpyAsync(c->d_tstate + t, src->d_tstate + st_, sizeof(TubeState), cudaMemcpyDeviceToDevice, c->stream));
   }
+  // clocks set before the first step (a resumed checkpoint)
+  for (int t = 0; t < c->ntubes; t++)
+    if (!c->clock_set.empty() && c->clock_set[t].first) {
+      TubeState ts;
+      memset(&ts, 0, sizeof(ts));
+      ts.Tm = c->clock_set[t].second.first;
+      ts.nstep = c->clock_set[t].second.second;
+      CK(cudaMemcpy(c->d_tstate + t, &ts, sizeof(ts), cudaMemcpyHostToDevice));
+    }
   for (int k = 0; k <= DS_NPHASE; k++) CK(cudaEventCreate(&c->ev[k]));
   CK(cudaStreamSynchronize(c->stream));
   c->finalized = true;
@@ -539,7 +550,9 @@ ds_status capture_graph(ds_ctx *c, int parity) {
 ds_status check_flags(ds_ctx *c) {
   int f = 0;
   CK(cudaMemcpy(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
-  if (f) return fail(c, DS_ERR_DEVICE, "device flags set: " + std::to_string(f));
+  // DS_FLAG_NONFINITE is reported, not an error: the reference's own runs can
+  // turn NaN (its eps guard, kernel.cu:2203) and go on
+  if (f & ~DS_FLAG_NONFINITE) return fail(c, DS_ERR_DEVICE, "device flags set: " + std::to_string(f));
   return DS_OK;
 }
 
@@ -867,10 +880,112 @@ ds_status ds_download_dust(ds_ctx *c, int species, double *x, double *y, double 
   return ds_get_dust(c, 0, species, x, y, z, vx, vy, vz, rho, t_stop, ind);
 }
 
+// ---------------------------------------------------------------------------
+// Binary checkpoints of one tube: "DSCKPT01", the tube's ds_params, its clock
+// (Tm, dt of the last step, step count), then per species the particle count
+// and every field in caller order (the fifteen FP64 fields, then Ind).
+// ---------------------------------------------------------------------------
+namespace {
+const char kCkptMagic[8] = {'D', 'S', 'C', 'K', 'P', 'T', '0', '1'};
+
+struct FileCloser {
+  FILE *f;
+  ~FileCloser() {
+    if (f) fclose(f);
+  }
+};
+}  // namespace
+
+ds_status ds_checkpoint_params(const char *path, ds_params *p) {
+  if (!path || !p) return DS_ERR_ARG;
+  FileCloser F{fopen(path, "rb")};
+  if (!F.f) return DS_ERR_IO;
+  char magic[8];
+  if (fread(magic, 1, 8, F.f) != 8 || memcmp(magic, kCkptMagic, 8) != 0) return DS_ERR_IO;
+  if (fread(p, sizeof(ds_params), 1, F.f) != 1) return DS_ERR_IO;
+  return DS_OK;
+}
+
+ds_status ds_save_tube(ds_ctx *c, int tube, const char *path) {
+  if (!c || !path) return DS_ERR_ARG;
+  if (!c->finalized) return fail(c, DS_ERR_STATE, "no resident state yet (call ds_step first)");
+  if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
+  double Tm = 0, dt = 0;
+  long long ns = 0;
+  ds_status st = ds_get_time(c, tube, &Tm, &dt, &ns);
+  if (st != DS_OK) return st;
+  const TubeDesc &T = c->tdesc[tube];
+  const int nsp = 1 + c->params[tube].n_dust;
+  FileCloser F{fopen(path, "wb")};
+  if (!F.f) return fail(c, DS_ERR_IO, std::string("cannot write ") + path);
+  bool ok = fwrite(kCkptMagic, 1, 8, F.f) == 8 && fwrite(&c->params[tube], sizeof(ds_params), 1, F.f) == 1 &&
+            fwrite(&Tm, sizeof Tm, 1, F.f) == 1 && fwrite(&dt, sizeof dt, 1, F.f) == 1 &&
+            fwrite(&ns, sizeof ns, 1, F.f) == 1 && fwrite(&nsp, sizeof nsp, 1, F.f) == 1;
+  for (int s = 0; ok && s < nsp; s++) {
+    const long long n = T.seg_end[s] - T.seg_begin[s];
+    std::vector<double> buf((size_t)NF * (size_t)(n > 0 ? n : 1));
+    std::vector<int> ind((size_t)(n > 0 ? n : 1));
+    double *f[NF];
+    for (int k = 0; k < NF; k++) f[k] = buf.data() + (size_t)k * (size_t)n;
+    if (n > 0 && (st = get_species(c, tube, s, f, ind.data())) != DS_OK) return st;
+    ok = fwrite(&n, sizeof n, 1, F.f) == 1 &&
+         (n == 0 || (fwrite(buf.data(), sizeof(double), (size_t)NF * n, F.f) == (size_t)NF * n &&
+                     fwrite(ind.data(), sizeof(int), (size_t)n, F.f) == (size_t)n));
+  }
+  if (!ok) return fail(c, DS_ERR_IO, std::string("short write to ") + path);
+  return DS_OK;
+}
+
+ds_status ds_load_tube(ds_ctx *c, int tube, const char *path) {
+  if (!c || !path) return DS_ERR_ARG;
+  if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
+  FileCloser F{fopen(path, "rb")};
+  if (!F.f) return fail(c, DS_ERR_IO, std::string("cannot read ") + path);
+  char magic[8];
+  ds_params P;
+  double Tm = 0, dt = 0;
+  long long ns = 0;
+  int nsp = 0;
+  if (fread(magic, 1, 8, F.f) != 8 || memcmp(magic, kCkptMagic, 8) != 0 || fread(&P, sizeof P, 1, F.f) != 1 ||
+      fread(&Tm, sizeof Tm, 1, F.f) != 1 || fread(&dt, sizeof dt, 1, F.f) != 1 || fread(&ns, sizeof ns, 1, F.f) != 1 ||
+      fread(&nsp, sizeof nsp, 1, F.f) != 1)
+    return fail(c, DS_ERR_IO, std::string("not a checkpoint: ") + path);
+  if (nsp != 1 + c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "checkpoint species count differs from the tube's");
+  for (int s = 0; s < nsp; s++) {
+    long long n = 0;
+    if (fread(&n, sizeof n, 1, F.f) != 1 || n < 0 || n > INT32_MAX) return fail(c, DS_ERR_IO, "truncated checkpoint");
+    std::vector<double> buf((size_t)NF * (size_t)(n > 0 ? n : 1));
+    std::vector<int> ind((size_t)(n > 0 ? n : 1));
+    if (n > 0 && (fread(buf.data(), sizeof(double), (size_t)NF * n, F.f) != (size_t)NF * n ||
+                  fread(ind.data(), sizeof(int), (size_t)n, F.f) != (size_t)n))
+      return fail(c, DS_ERR_IO, "truncated checkpoint");
+    const double *f[NF];
+    for (int k = 0; k < NF; k++) f[k] = buf.data() + (size_t)k * (size_t)n;
+    ds_status st = set_species(c, tube, s, (int)n, f, ind.data());
+    if (st != DS_OK) return st;
+  }
+  if (c->finalized) {  // resident context: set the clock now
+    TubeState ts;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&ts, c->d_tstate + tube, sizeof ts, cudaMemcpyDeviceToHost));
+    ts.Tm = Tm;
+    ts.nstep = ns;
+    CK(cudaMemcpy(c->d_tstate + tube, &ts, sizeof ts, cudaMemcpyHostToDevice));
+  } else {
+    if (c->clock_set.empty()) c->clock_set.assign(c->ntubes, {false, {0.0, 0LL}});
+    c->clock_set[tube] = {true, {Tm, ns}};
+  }
+  return DS_OK;
+}
+
 ds_status ds_get_time(ds_ctx *c, int tube, double *Tm, double *dt_last, long long *nsteps) {
   if (!c || tube < 0 || tube >= c->ntubes) return DS_ERR_ARG;
-  if (!c->finalized) {
-    if (Tm) *Tm = 0; if (dt_last) *dt_last = 0; if (nsteps) *nsteps = 0;
+  if (!c->finalized) {  // the clock a checkpoint set, else zero
+    const bool set = !c->clock_set.empty() && c->clock_set[tube].first;
+    if (Tm) *Tm = set ? c->clock_set[tube].second.first : 0.0;
+    if (dt_last) *dt_last = 0;
+    if (nsteps) *nsteps = set ? c->clock_set[tube].second.second : 0;
     return DS_OK;
   }
   TubeState ts;

@@ -450,7 +450,13 @@ __global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, con
       else if (z >= T.zmax) z = z - T.Lz;
     }
     st.x[i] = x; st.y[i] = y; st.z[i] = z;
-    if (s == 0) st.e[i] = st.e[i] + edot[i] * tau;
+    double e = 0.0;
+    if (s == 0) {
+      e = st.e[i] + edot[i] * tau;
+      st.e[i] = e;
+    }
+    if (!(isfinite(vx) && isfinite(vy) && isfinite(vz) && isfinite(x) && isfinite(y) && isfinite(z) && isfinite(e)))
+      atomicOr(flags, 4);  // DS_FLAG_NONFINITE
   }
 }
 

@@ -151,6 +151,44 @@ class Solver:
         _lib.check(self.L, self.ctx, self.L.ds_conservation(self.ctx, tube, _dp(out)), "ds_conservation")
         return out
 
+    def save(self, tube: int, path: str):
+        """Binary checkpoint of one tube (ds_save_tube)."""
+        _lib.check(self.L, self.ctx, self.L.ds_save_tube(self.ctx, tube, path.encode()), "ds_save_tube")
+
+    def load(self, tube: int, path: str):
+        """Restore one tube's particles and clock from a checkpoint (ds_load_tube)."""
+        st = self.L.ds_load_tube(self.ctx, tube, path.encode())
+        _lib.check(self.L, self.ctx, st, "ds_load_tube")
+        ps = _lib.DsParams()
+        _lib.check(self.L, None, self.L.ds_checkpoint_params(path.encode(), ctypes.byref(ps)), "ds_checkpoint_params")
+        self.n[tube] = [None] * (1 + int(ps.n_dust))
+        with open(path, "rb") as f:  # particle counts, from the file's species records
+            f.seek(8 + ctypes.sizeof(_lib.DsParams) + 3 * 8)
+            nsp = int(np.frombuffer(f.read(4), np.int32)[0])
+            for s in range(nsp):
+                n = int(np.frombuffer(f.read(8), np.int64)[0])
+                self.n[tube][s] = n
+                f.seek(n * (15 * 8 + 4), 1)
+
+    @classmethod
+    def from_checkpoint(cls, path: str) -> "Solver":
+        """A one-tube solver with the checkpoint's parameters, particles and clock."""
+        L = _lib.load()
+        ps = _lib.DsParams()
+        _lib.check(L, None, L.ds_checkpoint_params(path.encode(), ctypes.byref(ps)), "ds_checkpoint_params")
+        S = cls(_lib.params_from_c(ps))
+        S.load(0, path)
+        return S
+
+    def device_flags(self) -> int:
+        """Sticky device flags of the context (DS_FLAG_* bits of the ABI):
+        1 IDIC index out of range, 2 dust index beyond the gas count,
+        4 a non-finite velocity, position or energy."""
+        flags = ctypes.c_int(0)
+        msg = ctypes.create_string_buffer(512)
+        _lib.check(self.L, self.ctx, self.L.ds_last_error(self.ctx, ctypes.byref(flags), msg, 512), "ds_last_error")
+        return flags.value
+
     def dust_density(self):
         """Dust self-density of every tube at the current positions (the
         reference's output-only sweep, kernel.cu:2029-2043), on demand."""

@@ -37,7 +37,8 @@ typedef enum ds_status {
   DS_ERR_STATE = 3,    /* call out of order (e.g. step before particles are set) */
   DS_ERR_NOMEM = 4,    /* device allocation failed                                */
   DS_ERR_DEVICE = 5,   /* a kernel raised a sticky device-side flag               */
-  DS_ERR_UNSUPPORTED = 6
+  DS_ERR_UNSUPPORTED = 6,
+  DS_ERR_IO = 7        /* checkpoint file missing, unreadable or malformed         */
 } ds_status;
 
 /* Device-side flags (sticky per context, read with ds_last_error). */
@@ -46,6 +47,13 @@ typedef enum ds_status {
                                   kernel.cu:2116-2117); it was left unrelaxed   */
 #define DS_FLAG_PID_RANGE 0x2  /* dust index beyond the gas count in the index-
                                   coupled stopping time (IDIC.h:86)             */
+#define DS_FLAG_NONFINITE 0x4  /* a particle's velocity, position or energy became
+                                  NaN or infinite in a step.  Reported only: the
+                                  step succeeds and goes on, as the reference's
+                                  does (its cell key of a NaN position, int(NaN),
+                                  is undefined there; here the particle drops out
+                                  of the cell lists).  The other flags make
+                                  ds_step return DS_ERR_DEVICE.                 */
 
 /* Mode bits (ds_params.mode).  0 = the reference's own step. */
 #define DS_MODE_PERIODIC_Y 0x0001
@@ -202,6 +210,17 @@ ds_status ds_conservation(ds_ctx *c, int tube, double *out6);
  * this before ds_get_dust / ds_download_dust at output times instead of paying
  * for it every step (DS_MODE_DUST_RHO).  Same sums as the per-step sweep. */
 ds_status ds_dust_density(ds_ctx *c);
+
+/* Binary checkpoint of one tube.  The reference has none: its text snapshots
+ * print 8 decimals and cannot restart a run (kernel.cu:261).  The file holds the
+ * tube's ds_params, its clock (Tm, last dt, step count) and every particle field
+ * in caller order.  ds_checkpoint_params reads the parameters back, so a host can
+ * create a matching context; ds_load_tube restores particles and clock, before
+ * the first step or into a resident tube with the same particle counts.  On the
+ * FP64 path the resumed run equals the uninterrupted one bit for bit. */
+ds_status ds_save_tube(ds_ctx *c, int tube, const char *path);
+ds_status ds_checkpoint_params(const char *path, ds_params *p);
+ds_status ds_load_tube(ds_ctx *c, int tube, const char *path);
 
 /* Runs nsteps steps back to back (the graph's kernels, launched one by one)
  * with CUDA events between phases on the context's stream; returns the total

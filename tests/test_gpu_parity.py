@@ -86,6 +86,29 @@ def test_reference_mode_fp64_bitexact(name, nsteps):
     compare_exact(gpu, O.species, name)
 
 
+def test_nonfinite_flag_marks_the_reference_nan_onset():
+    """refA turns NaN at its third step (the reference's eps_2 guard defect,
+    kernel.cu:2203).  DS_FLAG_NONFINITE is clear while the oracle's moving
+    particles stay finite and set from the step where one of their velocities,
+    positions or energies first is not."""
+    g, P, sp = setup("refA")
+    O = OracleState(P, sp)
+    seen = False
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        for _ in range(5):
+            S.step(1)
+            O.step(1)
+            for k, q in enumerate(O.species):
+                m = q.ind == 0
+                fields = [q.vx, q.vy, q.vz, q.x, q.y, q.z] + ([q.e] if k == 0 else [])
+                seen = seen or not all(np.isfinite(f[m]).all() for f in fields)
+            assert bool(S.device_flags() & 4) == seen
+            if seen:
+                break
+    assert seen
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_gpu_replays_reference_snapshots(name):
     """The CUDA path against what the reference program itself printed."""
@@ -206,6 +229,42 @@ def test_dust_density_on_demand(precision):
         assert_equal_nan(d.rho, ref, "dust rho")
     else:
         assert np.abs(d.rho - ref).sum() / np.abs(ref).sum() < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_checkpoint_resume(precision, tmp_path):
+    """5 steps, checkpoint, a new solver from the file, 5 more steps = 10 steps
+    straight: bit for bit on the FP64 path (the step order depends only on the
+    caller order), relative L1 <= 1e-6 on the FP32 path (its cells keep their
+    previous slot order, which the checkpoint does not carry)."""
+    P, sp = small_tube()
+    P.precision = precision
+    path = str(tmp_path / "tube.ckpt")
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(5)
+        S.save(0, path)
+        t_saved = S.time(0)
+        S.step(5)
+        straight = [S.get_species(0, s) for s in range(2)]
+        t_straight = S.time(0)
+    R = Solver.from_checkpoint(path)
+    try:
+        t0 = R.time(0)
+        assert t0[0] == t_saved[0] and t0[2] == 5
+        R.step(5)
+        resumed = [R.get_species(0, s) for s in range(2)]
+        t_resumed = R.time(0)
+    finally:
+        R.close()
+    assert t_resumed[0] == t_straight[0] and t_resumed[2] == t_straight[2] == 10
+    for s in range(2):
+        for f in ("x", "vx", "rho"):
+            a, b = getattr(resumed[s], f), getattr(straight[s], f)
+            if precision == "fp64":
+                assert_equal_nan(a, b, f"species {s} {f}")
+            else:
+                assert np.abs(a - b).sum() / np.abs(b).sum() < 1e-6, (s, f)
 
 
 def test_batched_tubes_equal_single_runs():
