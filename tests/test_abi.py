@@ -64,3 +64,24 @@ def test_params_init_and_init_txt_reader(tmp_path):
 
 def test_version_string():
     assert b"sm_103a" in _lib.load().ds_version()
+
+
+def test_checkpoint_params_reads_the_header_and_rejects_bad_files(tmp_path):
+    """ds_checkpoint_params (file I/O only, no GPU): a file that starts with the
+    magic and a ds_params gives those parameters back; a missing, foreign or
+    truncated file gives DS_ERR_IO (7)."""
+    L = _lib.load()
+    P = _lib.DsParams()
+    assert L.ds_params_init(ctypes.byref(P)) == 0
+    P.h = 0.0123
+    P.n_dust = 1
+    good = tmp_path / "good.ckpt"
+    good.write_bytes(b"DSCKPT01" + bytes(P))
+    Q = _lib.DsParams()
+    assert L.ds_checkpoint_params(str(good).encode(), ctypes.byref(Q)) == 0
+    assert Q.h == 0.0123 and Q.n_dust == 1
+    for name, data in (("foreign", b"NOTACKPT" + bytes(P)), ("short", b"DSCKPT01" + bytes(P)[:10])):
+        f = tmp_path / name
+        f.write_bytes(data)
+        assert L.ds_checkpoint_params(str(f).encode(), ctypes.byref(Q)) == 7, name
+    assert L.ds_checkpoint_params(str(tmp_path / "missing").encode(), ctypes.byref(Q)) == 7
