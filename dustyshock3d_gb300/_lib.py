@@ -69,6 +69,8 @@ SIGNATURES = {
                       ctypes.c_int),
     "ds_kernels_per_step": ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "ds_dust_density": ([_VP], ctypes.c_int),
+    "ds_step_lists": ([_VP, ctypes.c_int, ctypes.c_int, _IP, _IP, _IP], ctypes.c_int),
+    "ds_get_fields": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_DP), _IP], ctypes.c_int),
     "ds_save_tube": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
     "ds_checkpoint_params": ([ctypes.c_char_p, ctypes.POINTER(DsParams)], ctypes.c_int),
     "ds_load_tube": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),

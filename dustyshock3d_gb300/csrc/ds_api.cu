@@ -63,6 +63,7 @@ struct ds_ctx {
   int N = 0;
   int nkeys = 0, key_bits = 0, nikeys = 0, ikey_bits = 0, ncell_total = 0, nseg = 0, nnseg = 0;
   int xl = 0;  // FP32 path: sub-cell x bits below the cell in the sort keys
+  int last_xl = 0;  // x bits of the keys of the last sort (0 after an exact-order sort)
   std::vector<TubeDesc> tdesc;
   std::vector<Chunk> ch_all, ch_gas, ch_dust;
   // device
@@ -294,6 +295,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   DevState dst = c->buf[c->parity ^ 1].view();
   const bool fast = c->any_fp32 && !exact_order;
   const int xl = fast ? c->xl : 0;  // fast keys carry the x bin below the cell
+  c->last_xl = xl;
   ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s);
   bool alt = false;
   ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt);
@@ -1031,8 +1033,8 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
     CK(cudaMalloc(&dh, sizeof(int) * (T.ncells + 1)));
     CK(cudaMalloc(&dn, sizeof(int) * (n > 0 ? n : 1)));
     CK(cudaMalloc(&dk, sizeof(int) * (n > 0 ? n : 1)));
-    ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, dh, dn,
-                          dk, c->stream);
+    ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, 0, dh,
+                          dn, dk, c->stream);
     CK(cudaGetLastError());
     if (head) CK(cudaMemcpyAsync(head, dh, sizeof(int) * (T.ncells + 1), cudaMemcpyDeviceToHost, c->stream));
     if (next && n) CK(cudaMemcpyAsync(next, dn, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -1041,6 +1043,36 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
     cudaFree(dh); cudaFree(dn); cudaFree(dk);
   }
   return DS_OK;
+}
+
+ds_status ds_step_lists(ds_ctx *c, int tube, int species, int *head, int *next, int *ncells) {
+  if (!c) return DS_ERR_ARG;
+  if (!c->finalized) return fail(c, DS_ERR_STATE, "no resident state yet (call ds_step first)");
+  if (tube < 0 || tube >= c->ntubes || species < 0 || species > c->params[tube].n_dust)
+    return fail(c, DS_ERR_ARG, "bad tube or species");
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  const int n = T.seg_end[species] - T.seg_begin[species];
+  if (ncells) *ncells = T.ncells;
+  if (!head && !next) return DS_OK;
+  int *dh = nullptr, *dn = nullptr, *dk = nullptr;
+  CK(cudaMalloc(&dh, sizeof(int) * (T.ncells + 1)));
+  CK(cudaMalloc(&dn, sizeof(int) * (n > 0 ? n : 1)));
+  CK(cudaMalloc(&dk, sizeof(int) * (n > 0 ? n : 1)));
+  // the slots still hold the last sort's order (the step moves particles in place)
+  ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, c->last_xl,
+                        dh, dn, dk, c->stream);
+  CK(cudaGetLastError());
+  if (head) CK(cudaMemcpyAsync(head, dh, sizeof(int) * (T.ncells + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (next && n) CK(cudaMemcpyAsync(next, dn, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(dh); cudaFree(dn); cudaFree(dk);
+  return DS_OK;
+}
+
+ds_status ds_get_fields(ds_ctx *c, int tube, int species, double *const *fields, int *ind) {
+  if (!c || !fields) return DS_ERR_ARG;
+  return get_species(c, tube, species, fields, ind);
 }
 
 ds_status ds_debug_idic(ds_ctx *c, int tube, int species, int *count, double *cells, int *ncells) {

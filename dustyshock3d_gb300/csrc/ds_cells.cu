@@ -541,7 +541,7 @@ __global__ void k_conservation(const TubeDesc *tubes, int tube, DevState st, dou
 // Reference linked lists of one segment from the sorted order: head[c] = pid
 // of the first slot of cell c, next[pid] = pid of the following slot in the
 // same cell (kernel.cu:1937-1955), plus the raw key per pid.
-__global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState st, const int *cell_start,
+__global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState st, const int *cell_start, int xl,
                               int *head, int *next, int *rawkey) {
   const TubeDesc &T = tubes[tube];
   const int b = T.seg_begin[s], e = T.seg_end[s];
@@ -553,7 +553,7 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c <= T.ncells) {
     const int kb = T.key_base[s];
-    const int j0 = cell_start[kb + c], j1 = cell_start[kb + c + 1];
+    const int j0 = cell_start[(kb + c) << xl], j1 = cell_start[(kb + c + 1) << xl];
     head[c] = j0 < j1 ? st.pid[j0] : -1;
     for (int j = j0; j < j1; j++) next[st.pid[j]] = (j + 1 < j1) ? st.pid[j + 1] : -1;
   }
@@ -694,10 +694,10 @@ void ds_launch_conservation(const TubeDesc *tubes, int tube, DevState st, double
   k_conservation<<<1, 256, 0, s>>>(tubes, tube, st, out);
 }
 void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nseg_particles, int ncells,
-                           DevState st, const int *cell_start, int *head, int *next, int *rawkey,
+                           DevState st, const int *cell_start, int xl, int *head, int *next, int *rawkey,
                            cudaStream_t s) {
   int n = nseg_particles > ncells + 1 ? nseg_particles : ncells + 1;
-  k_debug_lists<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, species, st, cell_start, head, next, rawkey);
+  k_debug_lists<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, species, st, cell_start, xl, head, next, rawkey);
 }
 void ds_launch_fill(double *a, int n, double v, cudaStream_t s) {
   if (n > 0) k_fill<<<blocks_for(n, 256), 256, 0, s>>>(a, n, v);

@@ -43,7 +43,8 @@ void ds_launch_dt(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t
 void ds_launch_step_end(TubeState *ts, int ntubes, cudaStream_t s);
 void ds_launch_conservation(const TubeDesc *tubes, int tube, DevState st, double *out, cudaStream_t s);
 void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nseg_particles, int ncells,
-                           DevState st, const int *cell_start, int *head, int *next, int *rawkey, cudaStream_t s);
+                           DevState st, const int *cell_start, int xl, int *head, int *next, int *rawkey,
+                           cudaStream_t s);
 
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, int xl, const double *h,
                            double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,

@@ -94,25 +94,37 @@ class Solver:
 
     # -- download -----------------------------------------------------------
     def get_species(self, tube: int, s: int, template: Species = None) -> Species:
+        """Every field of one species in caller order (ds_get_fields).  template
+        is accepted for older callers and not needed: m and h come back too."""
         n = self.n[tube][s]
-        out = {f: np.empty(n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "rho")}
+        names = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h", "ts")
+        out = {f: np.empty(n, np.float64) for f in names}
         ind = np.empty(n, np.int32)
-        if s == 0:
-            for f in ("ax", "ay", "az", "p", "e"):
-                out[f] = np.empty(n, np.float64)
-            st = self.L.ds_get_gas(self.ctx, tube, *[_dp(out[f]) for f in
-                                                     ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p",
-                                                      "e")], _ip(ind))
-        else:
-            out["ts"] = np.empty(n, np.float64)
-            st = self.L.ds_get_dust(self.ctx, tube, s, *[_dp(out[f]) for f in
-                                                         ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")], _ip(ind))
-        _lib.check(self.L, self.ctx, st, f"get species {s} of tube {tube}")
-        sp = Species(ind=ind, **out)
-        if template is not None:
-            sp.m = template.m.copy()
-            sp.h = None if template.h is None else template.h.copy()
-        return sp
+        ptrs = (_DP * len(names))(*[_dp(out[f]) for f in names])
+        _lib.check(self.L, self.ctx, self.L.ds_get_fields(self.ctx, tube, s, ptrs, _ip(ind)),
+                   f"get species {s} of tube {tube}")
+        return Species(ind=ind, **out)
+
+    def step_lists(self, tube: int, s: int):
+        """(head, next) of the cell lists the last step built (ds_step_lists)."""
+        n = self.n[tube][s]
+        nc = ctypes.c_int(0)
+        _lib.check(self.L, self.ctx, self.L.ds_step_lists(self.ctx, tube, s, None, None, ctypes.byref(nc)),
+                   "ds_step_lists")
+        head = np.empty(nc.value + 1, np.int32)
+        nxt = np.empty(max(n, 1), np.int32)
+        _lib.check(self.L, self.ctx, self.L.ds_step_lists(self.ctx, tube, s, _ip(head), _ip(nxt), ctypes.byref(nc)),
+                   "ds_step_lists")
+        return head, nxt[:n]
+
+    def write_snapshot(self, directory: str, num: int, tube: int = 0):
+        """The reference's snapshot files (Data_out / Data_out_dust) for one
+        tube, with the Nn columns from the last step's cell lists."""
+        from . import snapshot
+        P = self.params[tube]
+        species = [self.get_species(tube, s) for s in range(1 + P.n_dust)]
+        nexts = [self.step_lists(tube, s)[1] for s in range(1 + P.n_dust)]
+        snapshot.write(directory, num, self.time(tube)[0], P.tau, P.h, species, nexts)
 
     def time(self, tube: int = 0):
         Tm, dt = ctypes.c_double(), ctypes.c_double()

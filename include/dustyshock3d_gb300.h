@@ -200,6 +200,17 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
  * eps (dust).  *ncells receives n.  Any pointer may be NULL. */
 ds_status ds_debug_idic(ds_ctx *c, int tube, int species, int *count, double *cells, int *ncells);
 
+/* The cell lists of one species as the last step built them, before it moved
+ * the particles: what the reference's snapshot writer prints as Nn
+ * (kernel.cu:261, 463; its lists are built at the top of the step,
+ * kernel.cu:1937-1995).  Same layout as ds_debug_cells; no re-sort.  On the FP32
+ * path a cell lists its particles in the path's own slot order. */
+ds_status ds_step_lists(ds_ctx *c, int tube, int species, int *head, int *next, int *ncells);
+
+/* Every field of one species in caller order: fields[0..14] receive x, y, z,
+ * vx, vy, vz, ax, ay, az, rho, p, e, mas, h, t_stop (NULL entries skipped). */
+ds_status ds_get_fields(ds_ctx *c, int tube, int species, double *const *fields, int *ind);
+
 /* Global FP64 sums of one tube: out[0] mass, out[1..3] momentum, out[4] gas
  * internal energy sum m e, out[5] kinetic energy (all species). */
 ds_status ds_conservation(ds_ctx *c, int tube, double *out6);

@@ -310,3 +310,42 @@ def test_upload_download_roundtrip_preserves_order():
         c = S.get_species(0, 0)
     for f in ("x", "vx", "rho", "e"):
         assert_equal_nan(getattr(c, f), getattr(b, f), f)
+
+
+@pytest.mark.parametrize("name", ["refB", "refC"])
+def test_snapshot_files_replay_the_reference_output(name, tmp_path):
+    """The reference-format snapshot files written from the GPU state at the
+    reference's output steps hold what the reference program printed: every
+    column of every interior particle to the printed 8 decimals, and its cell
+    lists (the Nn column, from the lists of the step) exactly."""
+    g, P, sp = setup(name)
+    nsnap = len(g["snap_times"])
+    steps = snapshot_steps(P, nsnap)
+    cols_g = ["x", "y", "z", "r", "mas", "rho", "p", "Vx", "Vy", "Vy2", "V", "e", "Ind", "Nn"]
+    cols_d = ["x", "y", "z", "r", "mas", "rho", "t_stop", "Vx", "Vy", "Vy2", "V", "Ind", "Nn"]
+    interior = g["ind"] == 0
+
+    def read(path):
+        with open(path) as f:
+            lines = f.read().splitlines()
+        return lines, np.array([[float(v) for v in ln.split()] for ln in lines[3:] if ln.strip()])
+
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        done = 0
+        for s, st in enumerate(steps, start=1):
+            S.step(st - done)
+            done = st
+            S.write_snapshot(str(tmp_path), s)
+            lines, G = read(tmp_path / f"G{s:07d}.dat")
+            assert lines[0] == f"t={g['snap_times'][s - 1]:5.3f} "
+            assert (G[:, cols_g.index("Nn")].astype(np.int32) == g[f"s{s}_gas_Nn"]).all()
+            for c in ("x", "y", "z", "rho", "p", "Vx", "Vy", "V", "e"):
+                assert_close_nan(G[interior, cols_g.index(c)], g[f"s{s}_gas_{c}"], 1.01e-8, f"{name} s{s} G {c}")
+            for k in (1, 2):
+                _, D = read(tmp_path / f"D-{k}-{s:07d}.dat")
+                assert (D[:, cols_d.index("Nn")].astype(np.int32) == g[f"s{s}_d{k}_Nn"]).all()
+                for c in ("x", "y", "z", "rho", "t_stop", "Vx", "Vy", "V"):
+                    assert_close_nan(D[interior, cols_d.index(c)], g[f"s{s}_d{k}_{c}"], 1.01e-8,
+                                     f"{name} s{s} D-{k} {c}")
+            assert (tmp_path / f"L_X{s:07d}.dat").exists() and (tmp_path / f"D-2-L_X{s:07d}.dat").exists()
