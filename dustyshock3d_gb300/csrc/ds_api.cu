@@ -446,7 +446,7 @@ ds_status finalize(ds_ctx *c) {
   DA(c->cwb, (size_t)nkeys);
   DA(c->krad, (size_t)nkeys);
   CK(cudaMemsetAsync(c->krad, 1, (size_t)nkeys, c->stream));
-  DA(c->stage, N);
+  DA(c->stage, (size_t)NF * N + (N + 1) / 2 + 1);  // download staging: every field, then Ind
   if (c->any_fp32 && c->params[0].force_list != -1 && !c->ch_gas.empty()) {
     // the force sweep's neighbours, recorded by the gas density sweep
     c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : 256;
@@ -558,6 +558,44 @@ ds_status check_flags(ds_ctx *c) {
   return DS_OK;
 }
 
+// Host buffers that kernels may read or write in place: pinned and mapped
+// (cudaMallocHost, ds_host_alloc, cudaHostAlloc, mapped cudaHostRegister).
+// Their device address, else nullptr (pageable memory goes through the copy
+// engines).  On GB300 kernels reach such buffers over NVLink-C2C with many
+// loads in flight, well above what the copy engines give for many arrays.
+template <class T> T *mapped_ptr(const T *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear: an unknown pointer is simply not mapped
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? (T *)a.devicePointer : nullptr;
+}
+
+struct HostFields {
+  const double *src[NF];  // device addresses of mapped host arrays (nullptr: absent field)
+};
+
+// Upload of one segment straight from mapped host arrays, caller order (slot
+// b + p holds particle p; the next step sorts); absent fields: h the tube's h,
+// others zero.
+__global__ void k_upload_mapped(HostFields hf, const int *ind, int n, double hdef, DevState dst, int b) {
+  double *d[NF] = {dst.x, dst.y, dst.z, dst.vx, dst.vy, dst.vz, dst.ax, dst.ay, dst.az,
+                   dst.rho, dst.p, dst.e, dst.m, dst.h, dst.ts};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    // every load issued before any store: the link's latency is paid once
+    double v[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) v[f] = hf.src[f] ? hf.src[f][p] : (f == FH ? hdef : 0.0);
+    const int k = ind[p];
+#pragma unroll
+    for (int f = 0; f < NF; f++) d[f][b + p] = v[f];
+    dst.ind[b + p] = k;
+    dst.pid[b + p] = p;
+  }
+}
+
 ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fields, const int *ind) {
   if (!c) return DS_ERR_ARG;
   if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
@@ -587,6 +625,20 @@ ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fi
   CK(cudaSetDevice(c->device));
   Buffers &B = c->buf[c->parity];
   const int b = T.seg_begin[s];
+  {  // every given array mapped: one kernel reads them in place
+    HostFields hf;
+    bool all = n > 0;
+    for (int f = 0; f < NF && all; f++) {
+      hf.src[f] = mapped_ptr(fields[f]);
+      all = !fields[f] || hf.src[f];
+    }
+    const int *dind = all ? mapped_ptr(ind) : nullptr;
+    if (all && dind) {
+      k_upload_mapped<<<(n + 255) / 256, 256, 0, c->stream>>>(hf, dind, n, c->params[tube].h, B.view(), b);
+      CK(cudaGetLastError());
+      return DS_OK;
+    }
+  }
   for (int f = 0; f < NF; f++) {
     if (fields[f]) {
       CK(cudaMemcpyAsync(B.f[f] + b, fields[f], sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
@@ -604,13 +656,45 @@ ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fi
   return DS_OK;
 }
 
-__global__ void k_to_caller_order(const double *src, const int *pid, int b, int n, double *dst) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) dst[pid[b + q]] = src[b + q];
+// Download straight into mapped host arrays, written in caller order
+// (coalesced over the link): inv[p] = slot of particle p, then each thread p
+// reads its particle's slot.
+__global__ void k_slot_of(const int *pid, int b, int n, int *inv) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) inv[pid[b + q]] = q;
 }
-__global__ void k_to_caller_order_i(const int *src, const int *pid, int b, int n, int *dst) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) dst[pid[b + q]] = src[b + q];
+struct HostOut {
+  double *dst[NF];
+  const double *src[NF];
+  int nf;
+};
+__global__ void k_download_mapped(HostOut ho, const int *ind, int *ind_out, const int *inv, int b, int n) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int q = b + inv[p];
+    double v[NF];  // every load before any store
+#pragma unroll
+    for (int k = 0; k < NF; k++) v[k] = k < ho.nf ? ho.src[k][q] : 0.0;
+    const int i = ind_out ? ind[q] : 0;
+#pragma unroll
+    for (int k = 0; k < NF; k++)
+      if (k < ho.nf) ho.dst[k][p] = v[k];
+    if (ind_out) ind_out[p] = i;
+  }
+}
+
+// Every requested field of one segment back into caller order in one pass:
+// field k of the request (src[k]) to stage[k * n + pid], Ind to istage[pid].
+struct FieldSet {
+  const double *src[NF];
+  int nf;
+};
+__global__ void k_to_caller_order(FieldSet fs, const int *ind, const int *pid, int b, int n, double *stage,
+                                  int *istage) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = pid[b + q];
+  for (int k = 0; k < fs.nf; k++) stage[(size_t)k * n + p] = fs.src[k][b + q];
+  if (istage) istage[p] = ind[b + q];
 }
 
 ds_status get_species(ds_ctx *c, int tube, int s, double *const *out, int *ind_out) {
@@ -623,18 +707,43 @@ ds_status get_species(ds_ctx *c, int tube, int s, double *const *out, int *ind_o
   const int b = T.seg_begin[s], n = T.seg_end[s] - b;
   if (n == 0) return DS_OK;
   Buffers &B = c->buf[c->parity];
-  const int nb = (n + 255) / 256;
-  for (int f = 0; f < NF; f++) {
-    if (!out[f]) continue;
-    k_to_caller_order<<<nb, 256, 0, c->stream>>>(B.f[f], B.pid, b, n, c->stage);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(out[f], c->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  {  // every output mapped: write them in place
+    HostOut ho;
+    ho.nf = 0;
+    bool all = true;
+    for (int f = 0; f < NF && all; f++)
+      if (out[f]) {
+        ho.dst[ho.nf] = mapped_ptr(out[f]);
+        ho.src[ho.nf] = B.f[f];
+        all = ho.dst[ho.nf++] != nullptr;
+      }
+    int *dind = ind_out ? mapped_ptr(ind_out) : nullptr;
+    if (all && (!ind_out || dind)) {
+      int *inv = reinterpret_cast<int *>(c->stage + (size_t)NF * c->N);
+      k_slot_of<<<(n + 255) / 256, 256, 0, c->stream>>>(B.pid, b, n, inv);
+      k_download_mapped<<<(n + 255) / 256, 256, 0, c->stream>>>(ho, B.ind, dind, inv, b, n);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(c->stream));
+      return DS_OK;
+    }
   }
-  if (ind_out) {
-    k_to_caller_order_i<<<nb, 256, 0, c->stream>>>(B.ind, B.pid, b, n, (int *)c->stage);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(ind_out, c->stage, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
-  }
+  // one gather of every requested field into its own stage region, then the
+  // copies back to back (the copy engine streams without kernels in between)
+  FieldSet fs;
+  int map[NF];
+  fs.nf = 0;
+  for (int f = 0; f < NF; f++)
+    if (out[f]) {
+      map[fs.nf] = f;
+      fs.src[fs.nf++] = B.f[f];
+    }
+  int *istage = ind_out ? reinterpret_cast<int *>(c->stage + (size_t)NF * c->N) : nullptr;
+  k_to_caller_order<<<(n + 255) / 256, 256, 0, c->stream>>>(fs, B.ind, B.pid, b, n, c->stage, istage);
+  CK(cudaGetLastError());
+  for (int k = 0; k < fs.nf; k++)
+    CK(cudaMemcpyAsync(out[map[k]], c->stage + (size_t)k * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                       c->stream));
+  if (ind_out) CK(cudaMemcpyAsync(ind_out, istage, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return DS_OK;
 }

@@ -29,8 +29,9 @@ from .solver import Solver
 from .species import Species
 
 # device bytes per particle and per cell key of a batch context (ds_api.cu
-# allocations): two copies of 15 FP64 fields and 2 ints, FP32 copies, scratch
-BYTES_PER_PARTICLE = 2 * (15 * 8 + 8) + 3 * 16 + 4 * 8 + 14 * 4
+# allocations): two copies of 15 FP64 fields and 2 ints, FP32 copies, scratch,
+# the download staging (every field and Ind)
+BYTES_PER_PARTICLE = 2 * (15 * 8 + 8) + 3 * 16 + 4 * 8 + 14 * 4 + (15 * 8 + 4)
 BYTES_PER_KEY = 4 + 8 + 1
 BYTES_PER_IDIC_KEY = 4 + 14 * 8 + 4
 

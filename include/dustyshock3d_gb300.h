@@ -150,6 +150,13 @@ ds_status ds_set_dust(ds_ctx *c, int tube, int species, int n, const double *x, 
  * leave it (continuous batching), without the state leaving the GPU. */
 ds_status ds_copy_tube(ds_ctx *dst, int dst_tube, ds_ctx *src, int src_tube);
 
+/* Host buffers: pageable arrays go through the copy engines.  Pinned, mapped
+ * ones (ds_host_alloc, cudaMallocHost) are read and written in place by
+ * kernels over NVLink-C2C, in one pass per species: faster.  A resident upload
+ * from pinned buffers reads them asynchronously, so keep them unchanged until
+ * the next ds_step / ds_synchronize.  Downloads return when the data is in
+ * host memory either way. */
+
 /* Single-tube names the reference's host driver binds (tube 0). */
 ds_status ds_upload_gas(ds_ctx *c, int n, const double *x, const double *y, const double *z,
                         const double *vx, const double *vy, const double *vz, const double *ax,

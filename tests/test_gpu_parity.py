@@ -349,3 +349,60 @@ def test_snapshot_files_replay_the_reference_output(name, tmp_path):
                     assert_close_nan(D[interior, cols_d.index(c)], g[f"s{s}_d{k}_{c}"], 1.01e-8,
                                      f"{name} s{s} D-{k} {c}")
             assert (tmp_path / f"L_X{s:07d}.dat").exists() and (tmp_path / f"D-2-L_X{s:07d}.dat").exists()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pinned_upload_download_equal_pageable(precision):
+    """Pinned (mapped) host buffers take the in-place kernels, pageable ones the
+    copy engines; both give the same state bit for bit."""
+    import ctypes
+
+    from dustyshock3d_gb300 import _lib
+    P, sp = small_tube()
+    P.precision = precision
+    L = _lib.load()
+    keep = []
+
+    def pinned_copy(a):
+        ptr = ctypes.c_void_p()
+        assert L.ds_host_alloc(ctypes.byref(ptr), a.nbytes) == 0
+        keep.append(ptr)
+        out = np.frombuffer((ctypes.c_char * a.nbytes).from_address(ptr.value), dtype=a.dtype, count=a.size)
+        out[:] = a
+        return out
+
+    fields = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h", "ts")
+    try:
+        results = []
+        for pin in (False, True):
+            with Solver(P) as S:
+                S.set_tube(0, sp)
+                S.step(2)
+                got = [S.get_species(0, s) for s in range(2)]
+                if pin:  # re-upload the state from pinned buffers, then step on
+                    for s in range(2):
+                        q = got[s]
+                        for f in fields:
+                            setattr(q, f, pinned_copy(getattr(q, f)))
+                        q.ind = pinned_copy(q.ind)
+                        S.set_species(0, s, q)
+                else:
+                    for s in range(2):
+                        S.set_species(0, s, got[s])
+                S.step(2)
+                out = []
+                for s in range(2):
+                    n = S.n[0][s]
+                    bufs = {f: (pinned_copy(np.zeros(n)) if pin else np.zeros(n)) for f in fields}
+                    ind = pinned_copy(np.zeros(n, np.int32)) if pin else np.zeros(n, np.int32)
+                    ptrs = (ctypes.POINTER(ctypes.c_double) * 15)(
+                        *[bufs[f].ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for f in fields])
+                    assert L.ds_get_fields(S.ctx, 0, s, ptrs, ind.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
+                    out.append({**{f: bufs[f].copy() for f in fields}, "ind": ind.copy()})
+                results.append(out)
+        for s in range(2):
+            for f in fields + ("ind",):
+                assert_equal_nan(results[1][s][f], results[0][s][f], f"species {s} {f}")
+    finally:
+        for p in keep:
+            L.ds_host_free(p)
