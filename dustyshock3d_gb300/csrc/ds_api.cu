@@ -1270,7 +1270,7 @@ void ds_destroy(ds_ctx *c) {
 // whole device).  The sort's scratch (keys, values, their alternates and the
 // radix histograms) lives in the file-scope array below instead of in
 // context-owned memory.  It is sized for DS_NOALLOC_MAX_PARTICLES particles
-// (about 4.3 MB), and every GPU that loads this library holds it until the
+// (about 4.7 MB), and every GPU that loads this library holds it until the
 // process exits.  All calls share it: calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on it.  Every scratch
 // word a call reads has been written earlier in the same call, so nothing
@@ -1278,9 +1278,9 @@ void ds_destroy(ds_ctx *c) {
 // ===========================================================================
 namespace {
 
-constexpr int kNaTile = 2048;  // keys per radix tile (ds_sort.cu)
+constexpr int kNaTile = DS_RADIX_TILE;  // keys per radix tile (ds_sort.cu)
 constexpr int kNaMax = DS_NOALLOC_MAX_PARTICLES;
-constexpr size_t kNaHistWords = 256 * (size_t)((kNaMax + kNaTile - 1) / kNaTile) + 256;
+constexpr size_t kNaHistWords = DS_RADIX_BINS * (size_t)((kNaMax + kNaTile - 1) / kNaTile) + DS_RADIX_BINS;
 constexpr size_t kNaWords = 4 * (size_t)kNaMax + kNaHistWords;
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];

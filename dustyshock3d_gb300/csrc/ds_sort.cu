@@ -7,13 +7,14 @@
 // both orders equal to the reference's: the input is fed in caller-index
 // order, so equal keys keep ascending index.
 //
-// One pass per digit of <= 8 bits, three kernels per pass:
+// One pass per digit of <= 10 bits (as few passes as the key needs, digits as
+// narrow as they allow), three kernels per pass:
 //   rs_hist    per-tile digit histogram            -> hist[digit][tile]
 //   rs_rowscan per-digit exclusive scan over tiles -> hist (in place) + totals
 //   rs_scatter per-tile stable ranks (warp match-any + per-warp counters),
 //              global offset = scan(totals)[digit] + hist[digit][tile]
 // HBM traffic per pass: read key+value, write key+value (16 B per element)
-// plus 2 x 4 B x 256 per tile of histogram.
+// plus 2 x 4 B per digit value per tile of histogram.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -24,12 +25,21 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 8;                      // keys per thread
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // 2048 keys per tile
+static_assert(RS_TILE == DS_RADIX_TILE, "tile size is part of the scratch layout");
 constexpr int RS_WARP_SPAN = 32 * RS_ITEMS;      // contiguous keys handled by one warp
+#ifndef DS_RADIX_MAX_BITS
+#define DS_RADIX_MAX_BITS 10
+#endif
+constexpr int RS_MAX_BITS = DS_RADIX_MAX_BITS;
+constexpr int RS_BINS = 1 << RS_MAX_BITS;        // digit values at most
+static_assert(RS_BINS <= DS_RADIX_BINS, "histogram rows are sized for DS_RADIX_BINS digit values");
+constexpr int RS_DPT = RS_BINS / RS_THREADS;     // digit values per thread in the scatter's scan
 
 __global__ void __launch_bounds__(RS_THREADS) rs_hist(const uint32_t *__restrict__ keys, int n, int shift,
                                                       uint32_t mask, uint32_t *__restrict__ hist, int ntiles) {
-  __shared__ uint32_t h[256];
-  for (int t = threadIdx.x; t < 256; t += RS_THREADS) h[t] = 0;
+  __shared__ uint32_t h[RS_BINS];
+  const int nbins = (int)mask + 1;
+  for (int t = threadIdx.x; t < nbins; t += RS_THREADS) h[t] = 0;
   __syncthreads();
   const int base = blockIdx.x * RS_TILE;
   for (int k = threadIdx.x; k < RS_TILE; k += RS_THREADS) {
@@ -37,7 +47,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_hist(const uint32_t *__restrict
     if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = h[d];
+  for (int d = threadIdx.x; d < nbins; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = h[d];
 }
 
 // One block per digit: exclusive scan of hist[d][0..ntiles) and its total.
@@ -81,15 +91,24 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
                                                          int n, int shift, uint32_t mask,
                                                          const uint32_t *__restrict__ hist, int ntiles,
                                                          const uint32_t *__restrict__ totals) {
-  __shared__ uint32_t wcount[RS_WARPS][256];
-  __shared__ uint32_t goff[256];
-  __shared__ uint32_t wtot[8];
+  __shared__ uint32_t wcount[RS_WARPS][RS_BINS];
+  __shared__ uint32_t goff[RS_BINS];
+  __shared__ uint32_t wtot[RS_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int t = threadIdx.x; t < RS_WARPS * 256; t += RS_THREADS) (&wcount[0][0])[t] = 0;
-  // digit bases: exclusive scan of the 256 digit totals
+  const int nbins = (int)mask + 1;
+  for (int k = 0; k < RS_WARPS; k++)
+    for (int t = threadIdx.x; t < nbins; t += RS_THREADS) wcount[k][t] = 0;
+  // digit bases: exclusive scan of the digit totals, RS_DPT consecutive digit
+  // values per thread (thread order = digit order)
   {
-    uint32_t v = totals[threadIdx.x];  // RS_THREADS == 256
-    uint32_t s = v;
+    const int d0 = threadIdx.x * RS_DPT;
+    uint32_t v[RS_DPT], local = 0;
+#pragma unroll
+    for (int j = 0; j < RS_DPT; j++) {
+      v[j] = d0 + j < nbins ? totals[d0 + j] : 0u;
+      local += v[j];
+    }
+    uint32_t s = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
@@ -97,9 +116,13 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
     }
     if (lane == 31) wtot[w] = s;
     __syncthreads();
-    uint32_t pre = 0;
+    uint32_t pre = s - local;
     for (int k = 0; k < w; k++) pre += wtot[k];
-    goff[threadIdx.x] = pre + s - v + hist[(size_t)threadIdx.x * ntiles + blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < RS_DPT; j++) {
+      if (d0 + j < nbins) goff[d0 + j] = pre + hist[(size_t)(d0 + j) * ntiles + blockIdx.x];
+      pre += v[j];
+    }
   }
   __syncthreads();
 
@@ -112,7 +135,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
     const bool ok = i < n;
     key[r] = ok ? kin[i] : 0u;
     val[r] = ok ? vin[i] : 0u;
-    const uint32_t d = ok ? ((key[r] >> shift) & mask) : 0x100u;  // 0x100: no digit
+    const uint32_t d = ok ? ((key[r] >> shift) & mask) : (uint32_t)RS_BINS;  // RS_BINS: no digit
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const uint32_t before = ok ? wcount[w][d] : 0u;
     rank[r] = before + __popc(peers & lt_mask);
@@ -122,8 +145,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
   }
   __syncthreads();
   // exclusive prefix over warps (warps cover consecutive sub-ranges)
-  {
-    const int d = threadIdx.x;
+  for (int d = threadIdx.x; d < nbins; d += RS_THREADS) {
     uint32_t run = 0;
     for (int k = 0; k < RS_WARPS; k++) {
       uint32_t t = wcount[k][d];
@@ -148,10 +170,10 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
 size_t ds_radix_scratch_words(int n) {
   int ntiles = (n + RS_TILE - 1) / RS_TILE;
   if (ntiles < 1) ntiles = 1;
-  return (size_t)256 * ntiles + 256;
+  return (size_t)RS_BINS * ntiles + RS_BINS;
 }
 
-int ds_radix_passes(int key_bits) { return key_bits <= 0 ? 0 : (key_bits + 7) / 8; }
+int ds_radix_passes(int key_bits) { return key_bits <= 0 ? 0 : (key_bits + RS_MAX_BITS - 1) / RS_MAX_BITS; }
 
 cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, int n,
                           int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt) {
@@ -161,14 +183,14 @@ cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, ui
   const int width = (key_bits + passes - 1) / passes;
   const int ntiles = (n + RS_TILE - 1) / RS_TILE;
   uint32_t *hist = scratch;
-  uint32_t *totals = scratch + (size_t)256 * ntiles;
+  uint32_t *totals = scratch + (size_t)RS_BINS * ntiles;
   uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
   for (int p = 0; p < passes; p++) {
     const int shift = p * width;
     int bits = key_bits - shift < width ? key_bits - shift : width;
     const uint32_t mask = (1u << bits) - 1u;
     rs_hist<<<ntiles, RS_THREADS, 0, stream>>>(ki, n, shift, mask, hist, ntiles);
-    rs_rowscan<<<256, 256, 0, stream>>>(hist, ntiles, totals);
+    rs_rowscan<<<(int)mask + 1, 256, 0, stream>>>(hist, ntiles, totals);
     rs_scatter<<<ntiles, RS_THREADS, 0, stream>>>(ki, vi, ko, vo, n, shift, mask, hist, ntiles, totals);
     uint32_t *t = ki; ki = ko; ko = t;
     t = vi; vi = vo; vo = t;

@@ -4,6 +4,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+// Keys per radix tile and the most digit values of one pass (histogram rows).
+constexpr int DS_RADIX_TILE = 2048;
+constexpr int DS_RADIX_BINS = 1024;
+
 // 32-bit words of scratch the sort of n pairs needs.
 size_t ds_radix_scratch_words(int n);
 int ds_radix_passes(int key_bits);

@@ -268,7 +268,7 @@ ds_status ds_last_error(ds_ctx *c, int *device_flags, char *msg, int msglen);
  * ascending index, -1 at the end (kernel.cu:1937-1955) -- exactly as
  * ds_debug_cells reports them, without allocating anything.  The sort's
  * scratch is a static device array inside the library sized for
- * DS_NOALLOC_MAX_PARTICLES particles (about 4.3 MB per GPU that loads the
+ * DS_NOALLOC_MAX_PARTICLES particles (about 4.7 MB per GPU that loads the
  * library, held until the process exits); larger n returns DS_ERR_ARG.
  * Inputs and outputs are caller-owned device arrays: d_cell_key[n],
  * d_next[n], d_head[head_len] with head_len >= Number_of_fihd_cells + 1.
