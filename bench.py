@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--rate", type=float, default=4.0, help="serve: mean arrivals per second")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
+    ap.add_argument("--host-ic", action="store_true",
+                    help="serve: make initial particles on the host and upload them (default: on the device)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -504,9 +506,12 @@ def run_serve(args):
     import numpy as np
 
     from dustyshock3d_gb300 import ic
-    from dustyshock3d_gb300.serve import Server, poisson_requests
+    from dustyshock3d_gb300.serve import Server, device_uneven_tube, poisson_requests
     from dustyshock3d_gb300.solver import Solver
-    make = lambda rng: ic.uneven_tube(**ic.draw_tube_params(rng))  # noqa: E731
+    if args.host_ic:  # initial particles made on the host and uploaded at admission
+        make = lambda rng: ic.uneven_tube(**ic.draw_tube_params(rng))  # noqa: E731
+    else:  # generated on the device at admission (ds_init_tube)
+        make = device_uneven_tube
     reqs = poisson_requests(args.rate, args.requests, args.seed, make)
     clocks = ClockSampler(0)
     clocks.start()
@@ -523,14 +528,15 @@ def run_serve(args):
     P = mid.params.copy()
     P.T_end = 1e9
     with Solver(P) as S:
-        S.set_tube(0, mid.species)
+        mid.put(S, 0)
         S.step(2)
         ms, _ = S.step_timed(3)
     fp64_rate = mid.particles * 3 / (ms * 1e-3)
     line = {"metric": "particle-steps/s", "value": ps / wall, "unit": "particle-steps/s", "n_gpus": 1,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "serve", "requests": len(reqs), "rate_per_s": args.rate, "seed": args.seed,
-                       "budget_bytes": 150e9, "epoch_steps": 10, "t_end": "U[0.05, 0.2]"},
+                       "budget_bytes": 150e9, "epoch_steps": 10, "t_end": "U[0.05, 0.2]",
+                       "initial_conditions": "host" if args.host_ic else "device"},
             "p50_time_to_solution_s": float(np.percentile(tts, 50)),
             "p99_time_to_solution_s": float(np.percentile(tts, 99)), "wall_s": wall,
             "rebuilds": server.rebuilds, "particle_steps": ps,

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libdustyshock3d_gb300.so")
 
 DS_OK = 0
 STATUS = {0: "DS_OK", 1: "DS_ERR_ARG", 2: "DS_ERR_CUDA", 3: "DS_ERR_STATE", 4: "DS_ERR_NOMEM",
-          5: "DS_ERR_DEVICE", 6: "DS_ERR_UNSUPPORTED"}
+          5: "DS_ERR_DEVICE", 6: "DS_ERR_UNSUPPORTED", 7: "DS_ERR_IO"}
 DS_NPHASE = 4
 
 
@@ -39,6 +39,16 @@ class DsParams(ctypes.Structure):
     ]
 
 
+# ds_ic: initial conditions generated on the device (kinds DS_IC_*)
+IC_KINDS = {"sod_x_dust": 1, "sod_x_mas": 2, "dusty_sod": 3}
+IC_FIELDS = ("dx_left", "Ly", "Lz", "eps", "t_s", "rho_L", "p_L", "rho_R", "p_R", "gamma", "h_factor", "x0", "x1",
+             "wall", "lattice_offset", "t_end", "cfl", "alpha", "beta", "av_eps", "idic_cells", "fixed_tau")
+
+
+class DsIc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("reserved", ctypes.c_int)] + [(f, ctypes.c_double) for f in IC_FIELDS]
+
+
 _DP = ctypes.POINTER(ctypes.c_double)
 _IP = ctypes.POINTER(ctypes.c_int)
 _VP = ctypes.c_void_p
@@ -47,6 +57,10 @@ _VP = ctypes.c_void_p
 SIGNATURES = {
     "ds_params_init": ([ctypes.POINTER(DsParams)], ctypes.c_int),
     "ds_params_read_init_txt": ([ctypes.c_char_p, ctypes.POINTER(DsParams)], ctypes.c_int),
+    "ds_ic_init": ([ctypes.POINTER(DsIc), ctypes.c_int], ctypes.c_int),
+    "ds_ic_read_init_txt": ([ctypes.c_char_p, ctypes.POINTER(DsIc)], ctypes.c_int),
+    "ds_ic_plan": ([ctypes.POINTER(DsIc), ctypes.POINTER(DsParams), ctypes.POINTER(DsParams), _IP], ctypes.c_int),
+    "ds_init_tube": ([_VP, ctypes.c_int, ctypes.POINTER(DsIc)], ctypes.c_int),
     "ds_create": ([ctypes.POINTER(DsParams), ctypes.POINTER(_VP)], ctypes.c_int),
     "ds_create_batch": ([ctypes.c_int, ctypes.POINTER(DsParams), ctypes.POINTER(_VP)], ctypes.c_int),
     "ds_set_gas": ([_VP, ctypes.c_int, ctypes.c_int] + [_DP] * 14 + [_IP], ctypes.c_int),

@@ -123,6 +123,11 @@ _INIT_ORDER = [
 ]
 
 
+# extension names that take one number (the Init.txt fields may be set by name too)
+_FLOAT_FIELDS = {name for name, _ in _INIT_ORDER} | {"Gam_g", "Speed_of_sound_gas", "t_empty", "cell_w", "idic_w",
+                                                      "cfl"}
+
+
 def _leading_number(line: str, kind):
     """sscanf("%lf") / sscanf("%d") on one line: the leading number, rest ignored."""
     s = line.strip()
@@ -152,7 +157,11 @@ def parse_init_txt(text: str) -> Params:
         if not body or "=" not in body:
             continue
         key, val = (t.strip() for t in body.split("=", 1))
+        if key == "ic" or key.startswith("ic."):
+            continue  # initial conditions: ic.parse_ic_init_txt
         if key.startswith("mode."):
+            if key[5:] not in MODE_BITS:
+                raise ValueError(f"unknown mode switch {key!r}")
             setattr(P.mode, key[5:], val.lower() in ("1", "true", "yes", "on"))
         elif key in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             setattr(P, key, [float(v) for v in val.replace(",", " ").split()])
@@ -160,7 +169,7 @@ def parse_init_txt(text: str) -> Params:
             setattr(P, key, int(val))
         elif key == "precision":
             P.precision = val
-        elif hasattr(P, key):
+        elif key in _FLOAT_FIELDS:
             setattr(P, key, float(val))
         else:
             raise ValueError(f"unknown Init.txt extension {key!r}")

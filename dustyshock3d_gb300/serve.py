@@ -1,7 +1,7 @@
 """Continuous-batching server for shock-tube solves.
 
-Requests (a tube's parameters and initial particles, with an end time) arrive
-over time.  The server keeps every admitted tube's particle state resident on
+Requests (a tube's parameters and initial particles, or a generator that makes
+them on the device, with an end time) arrive over time.  The server keeps every admitted tube's particle state resident on
 the GPU and advances all of them together, one batch context, in epochs of
 ``epoch_steps`` steps (one CUDA graph replay per step).  Between epochs it
   * retires tubes that reached their end time (their state is downloaded and
@@ -11,7 +11,7 @@ the GPU and advances all of them together, one batch context, in epochs of
     tubes,
   * and, when the membership changed, rebuilds the batch: running tubes are
     carried into the new context device to device (``ds_copy_tube``), new ones
-    are uploaded.
+    are generated on the device (``ds_init_tube``) or uploaded.
 Each tube advances with its own CFL step and stops at its own end time, and
 nothing in a tube's arithmetic depends on the other tubes of the batch, so a
 request's result is the same alone and in the mix.
@@ -20,10 +20,11 @@ from __future__ import annotations
 
 import dataclasses
 import time
-from typing import Callable, List, Optional
+from typing import Callable, List, Optional, Sequence, Union
 
 import numpy as np
 
+from .ic import DeviceIC
 from .params import Params
 from .solver import Solver
 from .species import Species
@@ -54,8 +55,11 @@ def grid_sizes(P: Params):
     return ncells, nidic
 
 
-def memory_estimate(P: Params, species: List[Species]) -> int:
-    n = sum(s.n for s in species)
+def memory_estimate(P: Params, species: Sequence[Union[Species, int]]) -> int:
+    """Device bytes of one tube in a batch context; species: the species or
+    their particle counts (gas first)."""
+    counts = [s if isinstance(s, (int, np.integer)) else s.n for s in species]
+    n = sum(counts)
     ncells, nidic = grid_sizes(P)
     ns = 1 + P.n_dust
     b = n * BYTES_PER_PARTICLE + ns * (ncells + 2) * BYTES_PER_KEY + ns * (nidic + 2) * BYTES_PER_IDIC_KEY
@@ -63,22 +67,40 @@ def memory_estimate(P: Params, species: List[Species]) -> int:
         # recorded force neighbours: cap entries for every slot of the gas
         # chunks, a count per slot, a flag per chunk
         cap = P.force_list if P.force_list > 0 else 256
-        chunks = -(-species[0].n // 128)
+        chunks = -(-counts[0] // 128)
         b += chunks * 128 * 4 * cap + chunks + 4 * n
     return int(b)
 
 
 @dataclasses.dataclass
 class Request:
+    """A tube to solve: its initial particles (species), or ic, a generator run
+    on the device at admission (its plan gives params and the counts)."""
     rid: int
     arrival: float          # seconds after the start of the run
     params: Params
-    species: List[Species]
+    species: Optional[List[Species]]
     t_end: float
+    ic: Optional[DeviceIC] = None
+
+    @property
+    def counts(self) -> List[int]:
+        if self.species is not None:
+            return [s.n for s in self.species]
+        if not hasattr(self, "_counts"):
+            self._counts = self.ic.plan(self.params)[1]
+        return self._counts
 
     @property
     def particles(self) -> int:
-        return sum(s.n for s in self.species)
+        return sum(self.counts)
+
+    def put(self, S: Solver, tube: int):
+        """Place the initial particles into tube `tube` of S."""
+        if self.ic is not None:
+            S.init_tube(tube, self.ic)
+        else:
+            S.set_tube(tube, self.species)
 
 
 @dataclasses.dataclass
@@ -115,7 +137,7 @@ class Server:
 
     def estimate(self, r: Request) -> int:
         """Device bytes the request takes in this server's batch."""
-        return memory_estimate(self._params(r), r.species)
+        return memory_estimate(self._params(r), r.counts)
 
     def run(self, requests: List[Request], on_epoch: Optional[Callable] = None) -> List[Result]:
         pending = sorted(requests, key=lambda r: r.arrival)
@@ -141,7 +163,7 @@ class Server:
                 for t, r in enumerate(active):
                     Tm, _, nstep = S.time(t)
                     if Tm >= r.t_end:
-                        sp = [S.get_species(t, s, template=r.species[s]) for s in range(1 + r.params.n_dust)]
+                        sp = [S.get_species(t, s) for s in range(1 + r.params.n_dust)]
                         results.append(Result(r.rid, r.arrival, admitted_at[r.rid], self.clock() - t0, nstep,
                                               r.particles, sp))
                     else:
@@ -167,7 +189,7 @@ class Server:
                     for k, (t_old, r) in enumerate(keep):
                         N.copy_tube_from(k, S, t_old)
                     for k, r in enumerate(joined, start=len(keep)):
-                        N.set_tube(k, r.species)
+                        r.put(N, k)
                     N.step(0)  # make the carried tubes resident before the old context goes
                 else:
                     N = None
@@ -189,15 +211,27 @@ class Server:
 
 def poisson_requests(rate_per_s: float, n: int, seed: int, make_tube, t_end_range=(0.05, 0.2)) -> List[Request]:
     """n requests with exponential inter-arrival times (rate_per_s), seeded;
-    make_tube(rng) -> (params, species)."""
+    make_tube(rng) -> (params, species) or (params, DeviceIC)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     for i in range(n):
         t += float(rng.exponential(1.0 / rate_per_s))
         P, sp = make_tube(rng)
-        out.append(Request(i, t, P, sp, float(rng.uniform(*t_end_range))))
+        t_end = float(rng.uniform(*t_end_range))
+        if isinstance(sp, DeviceIC):
+            out.append(Request(i, t, P, None, t_end, ic=sp))
+        else:
+            out.append(Request(i, t, P, sp, t_end))
     return out
+
+
+def device_uneven_tube(rng):
+    """(params, DeviceIC) of one tube of the uneven-batch distributions
+    (ic.draw_tube_params), generated on the device at admission."""
+    from .ic import draw_tube_params
+    spec = DeviceIC.uneven(**draw_tube_params(rng))
+    return spec.plan()[0], spec
 
 
 def run_alone(r: Request, precision: str = "fp32") -> List[Species]:
@@ -206,7 +240,7 @@ def run_alone(r: Request, precision: str = "fp32") -> List[Species]:
     P.T_end = r.t_end
     P.precision = precision
     with Solver(P) as S:
-        S.set_tube(0, r.species)
+        r.put(S, 0)
         while S.time(0)[0] < r.t_end:
             S.step(50)
-        return [S.get_species(0, s, template=r.species[s]) for s in range(1 + P.n_dust)]
+        return [S.get_species(0, s) for s in range(1 + P.n_dust)]

@@ -76,6 +76,14 @@ class Solver:
         for s, sp in enumerate(species):
             self.set_species(tube, s, sp.copy().fill_missing())
 
+    def init_tube(self, tube: int, spec):
+        """Generate the tube's particles on the device (ds_init_tube); spec is an
+        ic.DeviceIC whose plan gave this tube's parameters."""
+        _lib.check(self.L, self.ctx, self.L.ds_init_tube(self.ctx, tube, ctypes.byref(spec.to_c())),
+                   f"ds_init_tube({spec.kind})")
+        _, counts = spec.plan(self.params[tube])
+        self.n[tube] = list(counts)
+
     # -- stepping -----------------------------------------------------------
     def step(self, n: int = 1):
         _lib.check(self.L, self.ctx, self.L.ds_step(self.ctx, int(n)), "ds_step")

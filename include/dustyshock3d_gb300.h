@@ -119,8 +119,94 @@ typedef struct ds_ctx ds_ctx;
 ds_status ds_params_init(ds_params *p);
 
 /* Parses an Init.txt the way the reference's main does (kernel.cu:1705-1723):
- * title line, then 17 positional values, trailing comments ignored. */
+ * title line, then 17 positional values, trailing comments ignored.  Lines
+ * after those (the reference never reads them) may set the extensions as
+ * "name = value", "//" starting a comment: any ds_params field by name
+ * (mass_ratio, R_dust, t_stop_const, eps_empty take up to DS_MAX_DUST values
+ * separated by spaces or commas; precision = fp32 | fp64), and "mode.<name> =
+ * 0 | 1" for each DS_MODE_* bit (mode.periodic_y, mode.h_per_particle, ...,
+ * mode.idic_proper).  "ic" lines belong to ds_ic_read_init_txt.  An unknown
+ * name or a malformed value is DS_ERR_ARG.  p keeps its values for fields the
+ * file does not set (start from ds_params_init). */
 ds_status ds_params_read_init_txt(const char *path, ds_params *p);
+
+/* Initial conditions generated on the device.  The reference's host driver
+ * fills its arrays with a generator before the upload (kernel.cu:1391); here
+ * the particles are generated straight into a tube's device state, so a run,
+ * or a served request, needs no host particle arrays.  Particles come out in
+ * the generators' own order and equal the host generators bit for bit.
+ *
+ *  DS_IC_SOD_X_DUST  init_Sod_X_Dust (kernel.cu:1391-1582), the generator the
+ *                    reference's main calls, from the Init.txt parameters:
+ *                    gas on two lattices of spacing (m / rho)^(1/3) (rho 1 | 1,
+ *                    e 2.5 | 2.0; m = 1 / Particle_on_length^3) accepted in
+ *                    |x| <= 1, |y|, |z| <= 0.8; two dust species on the gas
+ *                    sites (mass ratios 0.75, 0.5; R_dust 0.01, 1.0; t_stop
+ *                    from the gas p and rho, kernel.cu:43-46); sets n_dust 2,
+ *                    Coeff_h_dust_cell 0.5 and DS_MODE_REFERENCE.  Kept quirks:
+ *                    the interior (Ind = 0) test compares |y| with the x cube
+ *                    (kernel.cu:1441, 1481), and every lattice point, accepted
+ *                    or not, writes the Ind of the last accepted particle
+ *                    (kernel.cu:1441-1448).
+ *  DS_IC_SOD_X_MAS   the equal-mass lattices of init_Sod_X_mas (kernel.cu:938-
+ *                    1042: p 1 | 0.1, e 2.5 | 2.0, rho from Eq_State1, cube
+ *                    |x|, |y|, |z| <= 1), with the parameters' n_dust species
+ *                    of dust on the gas sites as init_Sod_X_Dust places them
+ *                    (kernel.cu:1505-1548, mass_ratio and R_dust of ds_params).
+ *  DS_IC_DUSTY_SOD   the dusty Sod shock tube (no reference counterpart): the
+ *                    ds_ic fields below.
+ * A rejected first lattice point (the reference then writes Ind_gas[-1]) and
+ * more gas particles than Maximum_particle (kernel.cu:1751) are DS_ERR_ARG. */
+#define DS_IC_SOD_X_DUST 1
+#define DS_IC_SOD_X_MAS 2
+#define DS_IC_DUSTY_SOD 3
+
+typedef struct ds_ic {
+  int kind;      /* DS_IC_*                                                        */
+  int reserved;
+  /* DS_IC_DUSTY_SOD: tube [x0, x1] x [0, Ly] x [0, Lz], periodic in y and z.  The
+     left state sits on a cubic lattice of spacing dx_left; the right lattice has
+     round(Ly / (dx_left (rho_L / rho_R)^(1/3))) sites across and the same particle
+     mass; h = h_factor x local spacing; gas sites at (i + lattice_offset) spacings
+     from the lower faces, one dust particle per gas site half a spacing further
+     (mass eps x the gas mass, constant stopping time t_s); particles within `wall`
+     smoothing lengths of an x end frozen (Ind 1).  The run parameters: periodic
+     y/z, per-particle h, CFL number cfl (or fixed_tau > 0), IDIC cells of
+     idic_cells right-lattice spacings, neighbour cells of 1.001 h_max, stencil 2,
+     FP64 (set precision and the like on the planned ds_params). */
+  double dx_left, Ly, Lz; /* Lz <= 0 -> Ly                                          */
+  double eps, t_s;
+  double rho_L, p_L, rho_R, p_R, gamma;
+  double h_factor;
+  double x0, x1, wall, lattice_offset;
+  double t_end, cfl, alpha, beta, av_eps;
+  double idic_cells;
+  double fixed_tau;
+} ds_ic;
+
+/* Defaults of a kind (DS_IC_DUSTY_SOD: Sod states 1, 1 | 0.125, 0.1; eps 1;
+ * t_s 1e-3; gamma 1.4; h_factor 1.3; x in [-0.5, 0.5]; wall 2.5; offset 0.25;
+ * t_end 0.2; cfl 0.3; alpha 1, beta 2, av_eps 0.01; idic_cells 2; dx_left and Ly
+ * left 0 for the caller). */
+ds_status ds_ic_init(ds_ic *ic, int kind);
+
+/* "ic = sod_x_dust | sod_x_mas | dusty_sod" and "ic.<field> = value" extension
+ * lines of an Init.txt (no "ic" line: DS_IC_SOD_X_DUST, as the reference). */
+ds_status ds_ic_read_init_txt(const char *path, ds_ic *ic);
+
+/* Host-side plan, no device work: the run parameters to create the context
+ * with (out; precision, stencil, force_list and the like may be changed before
+ * ds_create) and the particles per species (counts[1 + out->n_dust], gas
+ * first).  init: the Init.txt parameters the reference generators read (box,
+ * h, Particle_on_length, Type_of_state, Maximum_particle; for DS_IC_SOD_X_MAS
+ * also n_dust, mass_ratio, R_dust); may be NULL for DS_IC_DUSTY_SOD. */
+ds_status ds_ic_plan(const ds_ic *ic, const ds_params *init, ds_params *out, int *counts);
+
+/* Generates tube `tube`'s particles on the device, in place of ds_set_gas /
+ * ds_set_dust before the first step, or into a resident tube with the same
+ * particle counts (the clock is kept).  The tube's own parameters are the
+ * generator's init. */
+ds_status ds_init_tube(ds_ctx *c, int tube, const ds_ic *ic);
 
 /* One tube (the reference's single domain).  Replaces the reference's device
  * allocation and upload block (kernel.cu:1793-1926). */
@@ -176,7 +262,8 @@ ds_status ds_step(ds_ctx *c, int nsteps);
 ds_status ds_step_async(ds_ctx *c, int nsteps);
 ds_status ds_synchronize(ds_ctx *c);
 
-/* Downloads in the caller's index order; any pointer may be NULL (skipped). */
+/* Downloads in the caller's index order; any pointer may be NULL (skipped).
+ * Before the first step they return the particles as set (or generated). */
 ds_status ds_get_gas(ds_ctx *c, int tube, double *x, double *y, double *z, double *vx, double *vy,
                      double *vz, double *ax, double *ay, double *az, double *rho, double *p,
                      double *e, int *ind);

@@ -49,3 +49,26 @@ def test_budget_admits_one_at_a_time():
     for req, res in zip(reqs, results):
         alone = run_alone(req, "fp32")
         assert np.array_equal(res.species[0].rho, alone[0].rho)
+
+
+def test_device_generated_requests_equal_uploaded_requests():
+    """Requests whose particles the server generates on the device at admission
+    (ds_init_tube) finish with the same particles as the same tubes made on the
+    host and uploaded."""
+    shapes = [dict(N_gas=2.5e4, rho_ratio=8.0, p_ratio=10.0, eps=1.0, t_s=1e-3),
+              dict(N_gas=4.0e4, rho_ratio=5.0, p_ratio=7.0, eps=0.2, t_s=2e-2),
+              dict(N_gas=1.5e4, rho_ratio=12.0, p_ratio=15.0, eps=3.0, t_s=4e-4)]
+    host, dev = [], []
+    for i, kw in enumerate(shapes):
+        t_end = 0.01 + 0.005 * i
+        P, sp = ic.uneven_tube(**kw)
+        host.append(Request(i, 0.05 * i, P, sp, t_end=t_end))
+        spec = ic.DeviceIC.uneven(**kw)
+        dev.append(Request(i, 0.05 * i, spec.plan()[0], None, t_end=t_end, ic=spec))
+    a = Server(budget_bytes=150e9, epoch_steps=2, precision="fp32").run(host)
+    b = Server(budget_bytes=150e9, epoch_steps=2, precision="fp32").run(dev)
+    for ra, rb in zip(a, b):
+        assert ra.steps == rb.steps and ra.particles == rb.particles
+        for s in range(2):
+            for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "ind"):
+                assert np.array_equal(getattr(ra.species[s], f), getattr(rb.species[s], f)), (ra.rid, s, f)

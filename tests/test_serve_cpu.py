@@ -58,3 +58,21 @@ def test_request_larger_than_budget_is_refused():
     server = Server(budget_bytes=0.5 * Server(precision="fp32").estimate(reqs[0]), precision="fp32")
     with pytest.raises(ValueError, match="budget"):
         server.run(reqs)
+
+
+def test_device_generated_request_counts_and_estimate():
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300.serve import Request, device_uneven_tube
+    kw = dict(N_gas=3e4, rho_ratio=8.0, p_ratio=10.0, eps=1.0, t_s=1e-3)
+    P, sp = ic.uneven_tube(**kw)
+    spec = ic.DeviceIC.uneven(**kw)
+    r_host = Request(0, 0.0, P, sp, 0.1)
+    r_dev = Request(1, 0.0, spec.plan()[0], None, 0.1, ic=spec)
+    assert r_dev.counts == r_host.counts and r_dev.particles == r_host.particles
+    srv = Server(precision="fp32")
+    assert srv.estimate(r_dev) == srv.estimate(r_host)
+    # the seeded stream draws the same tubes either way
+    import numpy as np
+    a = device_uneven_tube(np.random.default_rng(5))
+    b_params, b_species = ic.uneven_tube(**ic.draw_tube_params(np.random.default_rng(5)))
+    assert a[1].plan()[1] == [s.n for s in b_species]
