@@ -39,7 +39,7 @@ sys.path.insert(0, ROOT)
 
 # Batched and served workloads (not the default line): 64 seeded uneven tubes,
 # and a Poisson stream of such tubes under a 150 GB budget.
-EXTRA_WORKLOADS = ("batch64", "serve", "accuracy_720k")
+EXTRA_WORKLOADS = ("batch64", "serve", "accuracy_720k", "initial_conditions")
 
 WORKLOADS = {
     # name: (dx_left, Ly, description)
@@ -631,6 +631,66 @@ def run_accuracy(args):
     return 0
 
 
+def run_ic(args):
+    """Initial conditions of the 720k and 5.76M tubes: made on the host (numpy,
+    ic.dusty_sod_tube) and uploaded at the first step, against generated on the
+    device (ds_init_tube) at the first step; and the regeneration of a resident
+    tube (plan + generator kernels + sync), median of args.steps.  The
+    generator writes 15 doubles and 2 ints per particle (128 B): its roofline
+    is HBM writes."""
+    import numpy as np
+
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300.solver import Solver
+    hbm, hbm_kind = peak_hbm()
+    clocks = ClockSampler(0)
+    clocks.start()
+    rows = []
+    for name in ("dusty_sod_720k", "dusty_sod_5760k"):
+        dx, Ly, desc = WORKLOADS[name]
+        kw = dict(dx_left=dx, Ly=Ly)
+        spec = ic.DeviceIC.dusty_sod(**kw)
+        P, counts = spec.plan()
+        P.precision = "fp32"
+        n = sum(counts)
+        t0 = time.perf_counter()
+        _, sp = ic.dusty_sod_tube(**kw)
+        t1 = time.perf_counter()
+        with Solver(P) as S:
+            S.set_tube(0, sp)
+            S.step(0)
+            t2 = time.perf_counter()
+        del sp
+        t3 = time.perf_counter()
+        with Solver(P) as S:
+            S.init_tube(0, spec)
+            S.step(0)
+            t4 = time.perf_counter()
+            for _ in range(max(3, args.warmup)):
+                S.init_tube(0, spec)
+            regen = []
+            for _ in range(max(5, args.steps)):
+                a = time.perf_counter()
+                S.init_tube(0, spec)
+                regen.append(time.perf_counter() - a)
+        r = float(np.median(regen))
+        rows.append({"workload": name, "particles": n, "host_generate_s": t1 - t0,
+                     "host_copies_and_upload_s": t2 - t1, "device_generate_and_setup_s": t4 - t3,
+                     "device_regenerate_s": r, "device_particles_per_s": n / r, "write_GBs": n * 128 / r / 1e9})
+    clk = clocks.stop()
+    big = rows[-1]
+    line = {"metric": "particles generated/s", "value": big["device_particles_per_s"], "unit": "particles/s",
+            "n_gpus": 1, "steps": max(5, args.steps), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "initial_conditions", "tubes": [r["workload"] for r in rows]},
+            "roofline": {"bound": "hbm", "achieved": big["write_GBs"], "peak": hbm, "unit": "GB/s",
+                         "frac": big["write_GBs"] / hbm, "traffic": None,
+                         "note": f"128 B written per particle; plan, launch and sync inside the time; peak {hbm_kind}"},
+            "tubes": rows, "gpu_launches": 2, "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -641,6 +701,8 @@ def main():
         return run_serve(args)
     if args.workload == "accuracy_720k":
         return run_accuracy(args)
+    if args.workload == "initial_conditions":
+        return run_ic(args)
     return run_ours(args)
 
 
