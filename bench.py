@@ -291,8 +291,15 @@ def force_bytes_per_particle(fp32: bool, hpp: bool) -> int:
     return 72 + (8 if hpp else 0) + 16 + 4 + 32
 
 
-def e2e_run(P, sp, steps, warmup):
-    """Full-state upload (pinned) + one step + full-state download, per step."""
+def e2e_run(P, sp, steps, warmup, bound=True):
+    """The metric end to end through the C ABI with the state on the host.
+
+    bound (the headline): the reference host's arrays, pinned, bound once with
+    ds_bind_host; each timed step is one ds_step_host(1) call that reads every
+    bound array from host memory, steps, and writes back what the step changed
+    (the transfers overlapped with the step's kernels).  Otherwise: per step
+    ds_upload_gas / ds_upload_dust from the same pinned arrays, ds_step(1),
+    ds_download_gas / ds_download_dust, each call returning before the next."""
     import ctypes
 
     import numpy as np
@@ -300,50 +307,43 @@ def e2e_run(P, sp, steps, warmup):
     from dustyshock3d_gb300 import _lib
     from dustyshock3d_gb300.solver import Solver
     L = _lib.load()
-    keep = []
-
-    def pinned(n, dtype):
-        ptr = ctypes.c_void_p()
-        nbytes = n * np.dtype(dtype).itemsize
-        _lib.check(L, None, L.ds_host_alloc(ctypes.byref(ptr), nbytes), "ds_host_alloc")
-        keep.append(ptr)
-        buf = (ctypes.c_char * nbytes).from_address(ptr.value)
-        return np.frombuffer(buf, dtype=dtype, count=n)
-
     S = Solver(P)
     S.set_tube(0, sp)
     g, d = sp[0].copy().fill_missing(), sp[1].copy().fill_missing()
-    gin = {f: pinned(g.n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p",
-                                                 "e", "m", "h")}
-    din = {f: pinned(d.n, np.float64) for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "m", "ts", "h")}
-    gind, dind = pinned(g.n, np.int32), pinned(d.n, np.int32)
+    GIN = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h")
+    DIN = ("x", "y", "z", "vx", "vy", "vz", "rho", "m", "ts", "h")
+    GOUT = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e")
+    DOUT = ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")
+    gin = {f: S.pinned(g.n) for f in GIN}
+    din = {f: S.pinned(d.n) for f in DIN}
+    gind, dind = S.pinned(g.n, np.int32), S.pinned(d.n, np.int32)
     for f, a in gin.items():
         a[:] = getattr(g, f)
     for f, a in din.items():
         a[:] = getattr(d, f)
     gind[:] = g.ind
     dind[:] = d.ind
-    gout = {f: gin[f] for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e")}
-    dout = {f: din[f] for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")}
+    h2d = sum(a.nbytes for a in gin.values()) + sum(a.nbytes for a in din.values()) + gind.nbytes + dind.nbytes
+    d2h = sum(gin[f].nbytes for f in GOUT) + sum(din[f].nbytes for f in DOUT)
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
     ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
-    h2d = sum(a.nbytes for a in gin.values()) + sum(a.nbytes for a in din.values()) + gind.nbytes + dind.nbytes
-    d2h = sum(a.nbytes for a in gout.values()) + sum(a.nbytes for a in dout.values()) + gind.nbytes + dind.nbytes
-
-    def one():
+    if bound:
+        S.bind_host(0, 0, gin, gind)
+        S.bind_host(0, 1, din, dind)
         c = S.ctx
-        _lib.check(L, c, L.ds_upload_gas(c, g.n, *[dp(gin[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay",
-                                                                         "az", "rho", "p", "e", "m", "h")], ip(gind)),
-                   "upload gas")
-        _lib.check(L, c, L.ds_upload_dust(c, 1, d.n, *[dp(din[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "rho",
-                                                                            "m", "ts", "h")], ip(dind)),
-                   "upload dust")
-        _lib.check(L, c, L.ds_step(c, 1), "step")
-        _lib.check(L, c, L.ds_download_gas(c, *[dp(gout[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay",
-                                                                      "az", "rho", "p", "e")], ip(gind)),
-                   "download gas")
-        _lib.check(L, c, L.ds_download_dust(c, 1, *[dp(dout[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "rho",
-                                                                          "ts")], ip(dind)), "download dust")
+
+        def one():
+            _lib.check(L, c, L.ds_step_host(c, 1), "ds_step_host")
+    else:
+        d2h += gind.nbytes + dind.nbytes  # the downloads return Ind too
+        c = S.ctx
+
+        def one():
+            _lib.check(L, c, L.ds_upload_gas(c, g.n, *[dp(gin[f]) for f in GIN], ip(gind)), "upload gas")
+            _lib.check(L, c, L.ds_upload_dust(c, 1, d.n, *[dp(din[f]) for f in DIN], ip(dind)), "upload dust")
+            _lib.check(L, c, L.ds_step(c, 1), "step")
+            _lib.check(L, c, L.ds_download_gas(c, *[dp(gin[f]) for f in GOUT], ip(gind)), "download gas")
+            _lib.check(L, c, L.ds_download_dust(c, 1, *[dp(din[f]) for f in DOUT], ip(dind)), "download dust")
 
     for _ in range(warmup):
         one()
@@ -352,8 +352,6 @@ def e2e_run(P, sp, steps, warmup):
         one()
     el = time.perf_counter() - t0
     S.close()
-    for p in keep:
-        L.ds_host_free(p)
     return el, h2d, d2h
 
 
@@ -411,11 +409,18 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         barrier(dist)
-        el, h2d, d2h = e2e_run(P32, sp, args.steps, min(args.warmup, 2))
+        el, h2d, d2h = e2e_run(P32, sp, args.steps, min(args.warmup, 2), bound=True)
         el = dist_max(dist, el)
         e2e = {"value": ws * n * args.steps / el, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / args.steps,
-               "path": "ds_upload_gas/dust (pinned) + ds_step(1) + ds_download_gas/dust, fp32 path"}
+               "path": "pinned host arrays bound once (ds_bind_host); per step ds_step_host(1): every bound "
+                       "array read, one step, the changed fields written back; fp32 path"}
+        barrier(dist)
+        el2, h2d2, d2h2 = e2e_run(P32, sp, args.steps, min(args.warmup, 2), bound=False)
+        el2 = dist_max(dist, el2)
+        e2e["separate_calls"] = {"value": ws * n * args.steps / el2, "h2d_bytes_per_step": h2d2,
+                                 "d2h_bytes_per_step": d2h2, "ms_per_step": 1e3 * el2 / args.steps,
+                                 "path": "ds_upload_gas/dust (pinned) + ds_step(1) + ds_download_gas/dust"}
     clk = clocks.stop()
 
     if rank != 0:

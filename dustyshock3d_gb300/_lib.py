@@ -71,6 +71,8 @@ SIGNATURES = {
     "ds_step": ([_VP, ctypes.c_int], ctypes.c_int),
     "ds_step_async": ([_VP, ctypes.c_int], ctypes.c_int),
     "ds_synchronize": ([_VP], ctypes.c_int),
+    "ds_bind_host": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_DP), _IP], ctypes.c_int),
+    "ds_step_host": ([_VP, ctypes.c_int], ctypes.c_int),
     "ds_get_gas": ([_VP, ctypes.c_int] + [_DP] * 12 + [_IP], ctypes.c_int),
     "ds_get_dust": ([_VP, ctypes.c_int, ctypes.c_int] + [_DP] * 8 + [_IP], ctypes.c_int),
     "ds_download_gas": ([_VP] + [_DP] * 12 + [_IP], ctypes.c_int),

@@ -39,6 +39,16 @@ struct HostSpecies {
 
 enum { FX, FY, FZ, FVX, FVY, FVZ, FAX, FAY, FAZ, FRHO, FP, FE, FM, FH, FTS, NF };
 
+// Host arrays bound to one species for ds_step_host: device addresses of
+// mapped host arrays (nullptr: field not bound), read by the kernels at run
+// time, so rebinding needs no new graph.
+struct BoundSeg {
+  double *f[NF];
+  int *ind;
+  int bound;     // 0: the segment is carried over from the resident state
+  int out_mask;  // fields written back after the step (bit f)
+};
+
 struct Buffers {
   double *f[NF] = {};
   int *ind = nullptr, *pid = nullptr;
@@ -103,6 +113,14 @@ struct ds_ctx {
   bool any_hpp = false, any_proper = false, any_dust_rho = false, any_fp32 = false;
   // graphs
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // host arrays bound to the step (ds_bind_host / ds_step_host)
+  std::vector<BoundSeg> hbound;  // [tube * DS_MAXS + species]
+  BoundSeg *d_bound = nullptr;
+  int *inv = nullptr;            // slot of each particle (absolute), all segments
+  bool any_bound = false;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t e_fork = nullptr, e_up = nullptr, e_dens = nullptr, e_force = nullptr, e_join = nullptr;
+  cudaGraphExec_t hgraph[2] = {nullptr, nullptr};
   // timing
   cudaEvent_t ev[DS_NPHASE + 1] = {};
   std::vector<cudaEvent_t> tev;
@@ -293,7 +311,7 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
 // Sort + reorder + cell ranges for the particles' current positions; flips
 // parity.  exact_order: cells list their particles in caller-index order even
 // on the FP32 path (the parity hook's lists).
-void enqueue_sort(ds_ctx *c, bool exact_order = false) {
+void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorder = nullptr) {
   cudaStream_t s = c->stream;
   DevState src = c->buf[c->parity].view();
   DevState dst = c->buf[c->parity ^ 1].view();
@@ -305,6 +323,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
   ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt);
   const uint32_t *skey = alt ? c->kalt : c->kin;
   const uint32_t *sval = alt ? c->valt : c->vin;
+  if (before_reorder) cudaStreamWaitEvent(s, before_reorder, 0);  // fields still arriving from the host
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
                     c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, fast, s);
   ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s);
@@ -316,7 +335,8 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false) {
 }
 
 // The step after the sort: sweeps, IDIC, update.  ev: optional phase events.
-void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
+void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullptr,
+                     cudaEvent_t after_force = nullptr) {
   cudaStream_t s = c->stream;
   bool alt = false;
   ds_radix_sort(c->ikin, c->ivin, c->ikalt, c->ivalt, c->N, c->ikey_bits, c->rs_scratch, s, &alt);
@@ -339,12 +359,14 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev) {
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
   }
   if (ev) cudaEventRecord(ev[2], s);
+  if (after_density) cudaEventRecord(after_density, s);
   DevState st = c->buf[c->parity].view();
   ds_launch_tstop(c->d_tubes, c->d_tstate, c->d_ch_dust, (int)c->ch_dust.size(), st, c->slot_of_pid, c->d_flags, s);
   ds_launch_dt(c->d_tubes, c->d_tstate, c->ntubes, s);
   if (fp32) ds_launch_force32(ag, c->any_hpp, depth, s);
   else ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
   if (ev) cudaEventRecord(ev[3], s);
+  if (after_force) cudaEventRecord(after_force, s);
   const uint32_t *ik = alt ? c->ikalt : c->ikin;
   const uint32_t *iv = alt ? c->ivalt : c->ivin;
   ds_launch_idic_reduce(ik, iv, c->N, c->nikeys, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st,
@@ -361,6 +383,113 @@ void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
   enqueue_sort(c);
   enqueue_physics(c, ev);
   if (ev) cudaEventRecord(ev[4], c->stream);
+}
+
+// ---------------------------------------------------------------------------
+// A step on bound host arrays (ds_step_host): the bound fields come in from the
+// host at the start, the changed ones go back as soon as the step has made
+// them final, on a second stream, overlapped with the step's own kernels.
+// ---------------------------------------------------------------------------
+
+// inv[seg_begin + pid[i]] = i: the slot of every particle, all segments
+__global__ void k_inverse(const Chunk *chunks, const TubeDesc *tubes, const int *pid, int *inv) {
+  const Chunk ch = chunks[blockIdx.x];
+  const int i = ch.begin + (int)threadIdx.x;
+  if (i >= ch.end) return;
+  inv[tubes[ch.tube].seg_begin[ch.species] + pid[i]] = i;
+}
+
+// Into the other buffer set in caller order (slot seg_begin + p = particle p):
+// bound fields from the host, unbound ones gathered from the resident state;
+// segments without host arrays carried over slot for slot.  PART 0: x, y, z
+// and pid (what the cell keys read); PART 1: the other fields and Ind.
+template <int PART>
+__global__ void k_bound_in(const Chunk *chunks, const TubeDesc *tubes, const BoundSeg *bs, const int *inv,
+                           DevState src, DevState dst) {
+  constexpr int F0 = PART == 0 ? 0 : 3, F1 = PART == 0 ? 3 : NF;
+  const Chunk ch = chunks[blockIdx.x];
+  const int i = ch.begin + (int)threadIdx.x;
+  if (i >= ch.end) return;
+  const BoundSeg &B = bs[ch.tube * DS_MAXS + ch.species];
+  const double *sf[NF] = {src.x, src.y, src.z, src.vx, src.vy, src.vz, src.ax, src.ay, src.az,
+                          src.rho, src.p, src.e, src.m, src.h, src.ts};
+  double *df[NF] = {dst.x, dst.y, dst.z, dst.vx, dst.vy, dst.vz, dst.ax, dst.ay, dst.az,
+                    dst.rho, dst.p, dst.e, dst.m, dst.h, dst.ts};
+  if (!B.bound) {
+#pragma unroll
+    for (int f = F0; f < F1; f++) df[f][i] = sf[f][i];
+    if (PART == 0) dst.pid[i] = src.pid[i];
+    else dst.ind[i] = src.ind[i];
+    return;
+  }
+  const int p = i - tubes[ch.tube].seg_begin[ch.species];
+  const int q = inv[i];  // the resident slot of particle p
+  double v[F1 - F0];     // every load before any store: the link's latency is paid once
+#pragma unroll
+  for (int f = F0; f < F1; f++) v[f - F0] = B.f[f] ? B.f[f][p] : sf[f][q];
+  int k = 0;
+  if (PART == 1) k = B.ind ? B.ind[p] : src.ind[q];
+#pragma unroll
+  for (int f = F0; f < F1; f++) df[f][i] = v[f - F0];
+  if (PART == 0) dst.pid[i] = p;
+  else dst.ind[i] = k;
+}
+
+// The bound fields a step has made final, back to the host in caller order:
+// PART 0 after the density sweeps (rho, p), 1 after the force sweep (ax, ay,
+// az, t_stop), 2 at the end (x, y, z, vx, vy, vz, e).
+template <int PART>
+__global__ void k_bound_out(const Chunk *chunks, const TubeDesc *tubes, const BoundSeg *bs, const int *inv,
+                            DevState st) {
+  constexpr int NOUT = PART == 0 ? 2 : (PART == 1 ? 4 : 7);
+  constexpr int fl0[2] = {FRHO, FP}, fl1[4] = {FAX, FAY, FAZ, FTS};
+  constexpr int fl2[7] = {FX, FY, FZ, FVX, FVY, FVZ, FE};
+  const Chunk ch = chunks[blockIdx.x];
+  const int i = ch.begin + (int)threadIdx.x;
+  if (i >= ch.end) return;
+  const BoundSeg &B = bs[ch.tube * DS_MAXS + ch.species];
+  if (!B.bound) return;
+  const double *sf[NF] = {st.x, st.y, st.z, st.vx, st.vy, st.vz, st.ax, st.ay, st.az,
+                          st.rho, st.p, st.e, st.m, st.h, st.ts};
+  const int p = i - tubes[ch.tube].seg_begin[ch.species];
+  const int q = inv[i];  // the slot of particle p after this step's sort
+  double v[NOUT];
+#pragma unroll
+  for (int k = 0; k < NOUT; k++) {
+    const int f = PART == 0 ? fl0[k] : (PART == 1 ? fl1[k] : fl2[k]);
+    v[k] = sf[f][q];
+  }
+#pragma unroll
+  for (int k = 0; k < NOUT; k++) {
+    const int f = PART == 0 ? fl0[k] : (PART == 1 ? fl1[k] : fl2[k]);
+    if (B.f[f] && (B.out_mask >> f & 1)) B.f[f][p] = v[k];
+  }
+}
+
+void enqueue_bound_step(ds_ctx *c) {
+  cudaStream_t s = c->stream, s2 = c->stream2;
+  const int nch = (int)c->ch_all.size();
+  const int P0 = c->parity;
+  DevState old = c->buf[P0].view(), neu = c->buf[P0 ^ 1].view();
+  k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, old.pid, c->inv);
+  cudaEventRecord(c->e_fork, s);
+  cudaStreamWaitEvent(s2, c->e_fork, 0);
+  k_bound_in<0><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, old, neu);
+  k_bound_in<1><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, old, neu);
+  cudaEventRecord(c->e_up, s2);
+  c->parity = P0 ^ 1;  // the caller-order state; the sort brings it back to P0
+  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, s);
+  enqueue_sort(c, false, c->e_up);
+  k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->buf[c->parity].pid, c->inv);
+  enqueue_physics(c, nullptr, c->e_dens, c->e_force);
+  DevState st = c->buf[c->parity].view();
+  cudaStreamWaitEvent(s2, c->e_dens, 0);
+  k_bound_out<0><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
+  cudaStreamWaitEvent(s2, c->e_force, 0);
+  k_bound_out<1><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
+  k_bound_out<2><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
+  cudaEventRecord(c->e_join, s2);
+  cudaStreamWaitEvent(s, c->e_join, 0);
 }
 
 ds_status finalize(ds_ctx *c) {
@@ -554,6 +683,27 @@ ds_status capture_graph(ds_ctx *c, int parity) {
   c->parity = saved;
   if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
   e = cudaGraphInstantiate(&c->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return DS_OK;
+}
+
+ds_status capture_bound_graph(ds_ctx *c, int parity) {
+  if (c->hgraph[parity]) return DS_OK;
+  const int saved = c->parity;
+  c->parity = parity;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_bound_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  const int after = c->parity;
+  c->parity = saved;
+  if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  if (after != parity) {
+    cudaGraphDestroy(g);
+    return fail(c, DS_ERR_STATE, "bound step: buffer parity not restored");
+  }
+  e = cudaGraphInstantiate(&c->hgraph[parity], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(c, DS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return DS_OK;
@@ -1192,6 +1342,69 @@ ds_status ds_step(ds_ctx *c, int nsteps) {
   return ds_synchronize(c);
 }
 
+ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *fields, int *ind) {
+  if (!c) return DS_ERR_ARG;
+  if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
+  if (species < 0 || species > c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "bad species index");
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  if (fields && n != T.seg_end[species] - T.seg_begin[species])
+    return fail(c, DS_ERR_ARG, "ds_bind_host: n differs from the tube's particle count");
+  BoundSeg B;
+  memset(&B, 0, sizeof(B));
+  if (fields) {
+    for (int f = 0; f < NF; f++)
+      if (fields[f]) {
+        B.f[f] = mapped_ptr(fields[f]);
+        if (!B.f[f]) return fail(c, DS_ERR_ARG, "ds_bind_host: arrays must be pinned host memory (ds_host_alloc, "
+                                                "cudaMallocHost or cudaHostRegister)");
+      }
+    if (ind) {
+      B.ind = mapped_ptr(ind);
+      if (!B.ind) return fail(c, DS_ERR_ARG, "ds_bind_host: ind must be pinned host memory");
+    }
+    B.bound = 1;
+    // written back: what a step changes in the reference's layout
+    B.out_mask = species == 0 ? (1 << FX | 1 << FY | 1 << FZ | 1 << FVX | 1 << FVY | 1 << FVZ | 1 << FAX | 1 << FAY |
+                                 1 << FAZ | 1 << FRHO | 1 << FP | 1 << FE)
+                              : (1 << FX | 1 << FY | 1 << FZ | 1 << FVX | 1 << FVY | 1 << FVZ | 1 << FRHO | 1 << FTS);
+  }
+  if (c->hbound.empty()) {
+    BoundSeg z;
+    memset(&z, 0, sizeof(z));
+    c->hbound.assign((size_t)c->ntubes * DS_MAXS, z);
+  }
+  if (!c->inv) DA(c->inv, c->N ? c->N : 1);
+  if (!c->d_bound) DA(c->d_bound, c->hbound.size());
+  if (!c->stream2) {
+    CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    cudaEvent_t *evs[] = {&c->e_fork, &c->e_up, &c->e_dens, &c->e_force, &c->e_join};
+    for (cudaEvent_t *e : evs) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  c->hbound[(size_t)tube * DS_MAXS + species] = B;
+  c->any_bound = false;
+  for (const BoundSeg &x : c->hbound) c->any_bound |= x.bound != 0;
+  CK(cudaStreamSynchronize(c->stream));  // no step reads the table while it changes
+  CK(cudaMemcpy(c->d_bound, c->hbound.data(), sizeof(BoundSeg) * c->hbound.size(), cudaMemcpyHostToDevice));
+  return DS_OK;
+}
+
+ds_status ds_step_host(ds_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  if (!c->any_bound) return fail(c, DS_ERR_STATE, "ds_step_host: no host arrays bound (ds_bind_host)");
+  CK(cudaSetDevice(c->device));
+  for (int k = 0; k < nsteps; k++) {
+    st = capture_bound_graph(c, c->parity);
+    if (st != DS_OK) return st;
+    CK(cudaGraphLaunch(c->hgraph[c->parity], c->stream));  // leaves the state in the same buffer set
+  }
+  return ds_synchronize(c);
+}
+
 ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms) {
   if (!c || nsteps < 0) return DS_ERR_ARG;
   ds_status st = finalize(c);
@@ -1534,8 +1747,14 @@ void ds_destroy(ds_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (int p = 0; p < 2; p++)
+  for (int p = 0; p < 2; p++) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
+    if (c->hgraph[p]) cudaGraphExecDestroy(c->hgraph[p]);
+  }
+  cudaEvent_t evs[] = {c->e_fork, c->e_up, c->e_dens, c->e_force, c->e_join};
+  for (cudaEvent_t e : evs)
+    if (e) cudaEventDestroy(e);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
   for (int k = 0; k <= DS_NPHASE; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (cudaEvent_t e : c->tev) cudaEventDestroy(e);

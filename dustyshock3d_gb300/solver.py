@@ -49,6 +49,7 @@ class Solver:
         _lib.check(self.L, None, st, "ds_create_batch")
         self.ctx = ctx
         self.n = [[None] * (1 + p.n_dust) for p in plist]
+        self._pinned = []  # host buffers from ds_host_alloc, freed with the solver
 
     # -- upload -------------------------------------------------------------
     def set_species(self, tube: int, s: int, sp: Species):
@@ -93,6 +94,37 @@ class Solver:
 
     def synchronize(self):
         _lib.check(self.L, self.ctx, self.L.ds_synchronize(self.ctx), "ds_synchronize")
+
+    # -- host arrays as the state of record ----------------------------------
+    def pinned(self, n: int, dtype=np.float64) -> np.ndarray:
+        """A numpy array in pinned host memory (ds_host_alloc), freed with the solver."""
+        dtype = np.dtype(dtype)
+        ptr = ctypes.c_void_p()
+        nbytes = max(1, n * dtype.itemsize)
+        _lib.check(self.L, None, self.L.ds_host_alloc(ctypes.byref(ptr), nbytes), "ds_host_alloc")
+        self._pinned.append(ptr)
+        buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+        return np.frombuffer(buf, dtype=dtype, count=n)
+
+    def bind_host(self, tube: int, s: int, arrays, ind=None):
+        """Bind pinned arrays (field name -> float64 array, the names of
+        Species; ind int32) to species s of a tube (ds_bind_host); arrays None
+        unbinds it."""
+        names = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h", "ts")
+        if arrays is None:
+            _lib.check(self.L, self.ctx, self.L.ds_bind_host(self.ctx, tube, s, 0, None, None), "ds_bind_host")
+            return
+        n = self.n[tube][s]
+        for f, a in arrays.items():
+            assert f in names and a.dtype == np.float64 and a.shape == (n,), f
+        assert ind is None or (ind.dtype == np.int32 and ind.shape == (n,))
+        self._bound = getattr(self, "_bound", {})
+        self._bound[(tube, s)] = (arrays, ind)  # keep the arrays alive while bound
+        ptrs = (_DP * len(names))(*[_dp(arrays.get(f)) for f in names])
+        _lib.check(self.L, self.ctx, self.L.ds_bind_host(self.ctx, tube, s, n, ptrs, _ip(ind)), "ds_bind_host")
+
+    def step_host(self, n: int = 1):
+        _lib.check(self.L, self.ctx, self.L.ds_step_host(self.ctx, int(n)), "ds_step_host")
 
     def step_timed(self, n: int = 1):
         tot = ctypes.c_float(0)
@@ -228,6 +260,9 @@ class Solver:
         if getattr(self, "ctx", None):
             self.L.ds_destroy(self.ctx)
             self.ctx = None
+        for ptr in getattr(self, "_pinned", []):
+            self.L.ds_host_free(ptr)
+        self._pinned = []
 
     def __del__(self):
         try:

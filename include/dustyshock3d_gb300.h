@@ -262,6 +262,26 @@ ds_status ds_step(ds_ctx *c, int nsteps);
 ds_status ds_step_async(ds_ctx *c, int nsteps);
 ds_status ds_synchronize(ds_ctx *c);
 
+/* Host arrays as the state of record, the way the reference's host keeps its
+ * data.h arrays between steps.  ds_bind_host binds caller-owned pinned arrays
+ * (ds_host_alloc, cudaMallocHost, or cudaHostRegister'ed) to one species of
+ * one tube: fields[0..14] = x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, mas,
+ * h, t_stop as in ds_get_fields, n = the species' particle count, ind its Ind.
+ * ds_step_host then runs nsteps steps; each reads every bound array (the
+ * caller may change them between calls) and writes back what the step
+ * changes -- gas x..e (12 fields), dust x, y, z, vx, vy, vz, rho, t_stop --
+ * in the caller's index order.  NULL entries are neither read nor written
+ * (the resident values stay), and species left unbound stay resident.  Inside
+ * a step the reads of the fields other than x, y, z overlap the cell sort,
+ * and rho, p go back during the force sweep, ax, ay, az, t_stop during the
+ * IDIC phase (kernels over NVLink-C2C on a second stream, all in one CUDA
+ * graph).  Returns when the last step's results are in host memory.  Results
+ * equal ds_upload_* + ds_step(1) + ds_download_* per step, bit for bit.
+ * fields == NULL unbinds the species.  ds_step / ds_get_* keep working on the
+ * resident state in between. */
+ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *fields, int *ind);
+ds_status ds_step_host(ds_ctx *c, int nsteps);
+
 /* Downloads in the caller's index order; any pointer may be NULL (skipped).
  * Before the first step they return the particles as set (or generated). */
 ds_status ds_get_gas(ds_ctx *c, int tube, double *x, double *y, double *z, double *vx, double *vy,

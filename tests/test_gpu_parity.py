@@ -312,12 +312,15 @@ def test_upload_download_roundtrip_preserves_order():
         assert_equal_nan(getattr(c, f), getattr(b, f), f)
 
 
+@pytest.mark.parametrize("source", ["host", "device"])
 @pytest.mark.parametrize("name", ["refB", "refC"])
-def test_snapshot_files_replay_the_reference_output(name, tmp_path):
+def test_snapshot_files_replay_the_reference_output(name, source, tmp_path):
     """The reference-format snapshot files written from the GPU state at the
     reference's output steps hold what the reference program printed: every
     column of every interior particle to the printed 8 decimals, and its cell
-    lists (the Nn column, from the lists of the step) exactly."""
+    lists (the Nn column, from the lists of the step) exactly.  source
+    "device": the initial particles are generated on the device from the same
+    Init.txt (ds_init_tube, init_Sod_X_Dust) instead of uploaded."""
     g, P, sp = setup(name)
     nsnap = len(g["snap_times"])
     steps = snapshot_steps(P, nsnap)
@@ -330,8 +333,15 @@ def test_snapshot_files_replay_the_reference_output(name, tmp_path):
             lines = f.read().splitlines()
         return lines, np.array([[float(v) for v in ln.split()] for ln in lines[3:] if ln.strip()])
 
+    if source == "device":
+        from dustyshock3d_gb300 import ic, parse_init_txt
+        spec = ic.DeviceIC(kind="sod_x_dust")
+        P = spec.plan(parse_init_txt(str(g["init_txt"])))[0]
     with Solver(P) as S:
-        S.set_tube(0, sp)
+        if source == "device":
+            S.init_tube(0, spec)
+        else:
+            S.set_tube(0, sp)
         done = 0
         for s, st in enumerate(steps, start=1):
             S.step(st - done)
