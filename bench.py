@@ -324,7 +324,11 @@ def e2e_run(P, sp, steps, warmup, bound=True):
     gind[:] = g.ind
     dind[:] = d.ind
     h2d = sum(a.nbytes for a in gin.values()) + sum(a.nbytes for a in din.values()) + gind.nbytes + dind.nbytes
-    d2h = sum(gin[f].nbytes for f in GOUT) + sum(din[f].nbytes for f in DOUT)
+    if bound:  # what ds_step_host writes back (dust rho and t_stop only where the step can change them)
+        dout = [f for f in DOUT if (f != "rho" or P.mode.dust_rho) and (f != "ts" or not P.mode.tstop_const)]
+    else:
+        dout = DOUT
+    d2h = sum(gin[f].nbytes for f in GOUT) + sum(din[f].nbytes for f in dout)
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
     ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
     if bound:

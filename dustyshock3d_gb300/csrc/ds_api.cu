@@ -1366,10 +1366,14 @@ ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *f
       if (!B.ind) return fail(c, DS_ERR_ARG, "ds_bind_host: ind must be pinned host memory");
     }
     B.bound = 1;
-    // written back: what a step changes in the reference's layout
+    // written back: what a step can change in the reference's layout (dust rho
+    // only with the per-step dust density, t_stop only when not constant)
+    const int mode = c->params[tube].mode;
     B.out_mask = species == 0 ? (1 << FX | 1 << FY | 1 << FZ | 1 << FVX | 1 << FVY | 1 << FVZ | 1 << FAX | 1 << FAY |
                                  1 << FAZ | 1 << FRHO | 1 << FP | 1 << FE)
-                              : (1 << FX | 1 << FY | 1 << FZ | 1 << FVX | 1 << FVY | 1 << FVZ | 1 << FRHO | 1 << FTS);
+                              : (1 << FX | 1 << FY | 1 << FZ | 1 << FVX | 1 << FVY | 1 << FVZ |
+                                 ((mode & DS_MODE_DUST_RHO) ? 1 << FRHO : 0) |
+                                 ((mode & DS_MODE_TSTOP_CONST) ? 0 : 1 << FTS));
   }
   if (c->hbound.empty()) {
     BoundSeg z;

@@ -415,6 +415,9 @@ __device__ __forceinline__ void ds_walk(const TubeDesc &T, const Stencil &S, boo
 #define DS_NOFS32 243
 #define DS_OFS32_SHIFT 24
 #define DS_SLOT32_MASK ((1u << DS_OFS32_SHIFT) - 1u)
+#ifndef DS_XWIN_MARGIN
+#define DS_XWIN_MARGIN 0.01f  // fine x bins added on each side of a lane's row window
+#endif
 #ifndef DS_RPIECE
 #define DS_RPIECE 8  // candidates of a row screened together (measured: 8 beats 4 and 6)
 #endif
@@ -455,11 +458,13 @@ __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S
   const int bi = S.ix >> DS_XB_LOG;
   const int cx0 = S.ix - r < 0 ? 0 : S.ix - r;
   const int cx1 = S.ix + r > T.nx - 1 ? T.nx - 1 : S.ix + r;
-  // the window in fine x indices (cell << xl | bin), clipped to the row
+  // the window in fine x indices (cell << xl | bin), clipped to the row; the
+  // margin covers a partner whose FP64 key put it in the next bin (the FP32
+  // window and the FP64 keys disagree by ~1e-5 of a bin at most)
   const float sc = (float)(1 << xl) * (float)T.inv_wx;
   const int fb = (bi * DS_XB) << xl;  // fine index of the own block's origin
-  int f_lo = fb + (int)floorf((pi.x - cutx) * sc) - 1;
-  int f_hi = fb + (int)floorf((pi.x + cutx) * sc) + 1;
+  int f_lo = fb + (int)floorf((pi.x - cutx) * sc - DS_XWIN_MARGIN);
+  int f_hi = fb + (int)floorf((pi.x + cutx) * sc + DS_XWIN_MARGIN);
   f_lo = f_lo < (cx0 << xl) ? (cx0 << xl) : f_lo;
   f_hi = f_hi > ((cx1 + 1) << xl) - 1 ? ((cx1 + 1) << xl) - 1 : f_hi;
   const int bsplit = (f_hi >> (xl + DS_XB_LOG)) << (xl + DS_XB_LOG);  // first fine index of f_hi's block

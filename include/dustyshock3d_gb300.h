@@ -268,9 +268,10 @@ ds_status ds_synchronize(ds_ctx *c);
  * one tube: fields[0..14] = x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, mas,
  * h, t_stop as in ds_get_fields, n = the species' particle count, ind its Ind.
  * ds_step_host then runs nsteps steps; each reads every bound array (the
- * caller may change them between calls) and writes back what the step
- * changes -- gas x..e (12 fields), dust x, y, z, vx, vy, vz, rho, t_stop --
- * in the caller's index order.  NULL entries are neither read nor written
+ * caller may change them between calls) and writes back what the step can
+ * change -- gas x..e (12 fields); dust x, y, z, vx, vy, vz, rho (with
+ * DS_MODE_DUST_RHO) and t_stop (without DS_MODE_TSTOP_CONST) -- in the
+ * caller's index order.  NULL entries are neither read nor written
  * (the resident values stay), and species left unbound stay resident.  Inside
  * a step the reads of the fields other than x, y, z overlap the cell sort,
  * and rho, p go back during the force sweep, ax, ay, az, t_stop during the
