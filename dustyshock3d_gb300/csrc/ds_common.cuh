@@ -442,8 +442,15 @@ __device__ __forceinline__ void ds_fill_shift_table32(const TubeDesc &T, float4 
 // half-rows instead of cells): rows (l, g) in [-r, r]^2, l outer; within a row
 // ascending slot.  The sort keys carry T.xl bits of x within the cell, so a
 // row's slots are sorted by x and cell_start (indexed by cell << xl | bin)
-// bounds the lane's x window [x - cutx, x + cutx] (one bin of slack each
-// side) instead of the whole row: every lane's window has the same length.
+// bounds the lane's x window instead of the whole row.  cutx bounds the
+// distance of every partner the screen can accept.  On a proper grid the rows
+// are true (y, z) rows, so of row (l, g) a lane needs only the x within
+// sqrt(cutx^2 - d^2) of its own, d its distance to the row's y-z rectangle,
+// and nothing of a row farther than cutx: the window shrinks toward the outer
+// rows (a relative margin of 1e-4 on cutx^2 keeps FP32 rounding out of it).
+// Dropped candidates lie outside the cut-off sphere, so the accepted pairs and
+// their order are those of the full rows.  A row crossing an x-block edge is
+// two ranges; the second pass runs only when some lane's window crosses one.
 // screen(slot, ox, oy, oz) gets the range's shift minus the particle's own
 // FP32 coordinates; use(slot, code) runs over the survivors.
 template <int CAP, class Screen, class Use>
@@ -452,23 +459,21 @@ __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S
                                              const float4 *shtab, uint32_t *lst, Screen screen, Use use) {
   const unsigned FULL = 0xffffffffu;
   const int w = 2 * r + 1;
-  const int nq = act ? 2 * w * w : 0;
-  const int nq_w = __reduce_max_sync(FULL, nq);
+  const int nrow = act ? w * w : 0;
+  const int nrow_w = __reduce_max_sync(FULL, nrow);
   const int xl = T.xl;
   const int bi = S.ix >> DS_XB_LOG;
   const int cx0 = S.ix - r < 0 ? 0 : S.ix - r;
   const int cx1 = S.ix + r > T.nx - 1 ? T.nx - 1 : S.ix + r;
-  // the window in fine x indices (cell << xl | bin), clipped to the row; the
-  // margin covers a partner whose FP64 key put it in the next bin (the FP32
-  // window and the FP64 keys disagree by ~1e-5 of a bin at most)
+  // windows in fine x indices (cell << xl | bin), clipped to the rows' cells;
+  // the margin covers a partner whose FP64 key put it in the next bin (the
+  // FP32 window and the FP64 keys disagree by ~1e-5 of a bin at most)
   const float sc = (float)(1 << xl) * (float)T.inv_wx;
   const int fb = (bi * DS_XB) << xl;  // fine index of the own block's origin
-  int f_lo = fb + (int)floorf((pi.x - cutx) * sc - DS_XWIN_MARGIN);
-  int f_hi = fb + (int)floorf((pi.x + cutx) * sc + DS_XWIN_MARGIN);
-  f_lo = f_lo < (cx0 << xl) ? (cx0 << xl) : f_lo;
-  f_hi = f_hi > ((cx1 + 1) << xl) - 1 ? ((cx1 + 1) << xl) - 1 : f_hi;
-  const int bsplit = (f_hi >> (xl + DS_XB_LOG)) << (xl + DS_XB_LOG);  // first fine index of f_hi's block
-  const bool split = bsplit > f_lo;
+  const int fmin = cx0 << xl, fmax = ((cx1 + 1) << xl) - 1;
+  const bool narrow = (T.mode & M_GRID_PROPER) != 0;
+  const float c2 = cutx * cutx * 1.0001f;
+  const float wy = (float)T.wy, wz = (float)T.wz;
   int n = 0;
   auto flush = [&]() {
     const int nw = __reduce_max_sync(FULL, n);
@@ -480,18 +485,38 @@ __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S
     n = 0;
   };
   int l = -r, g = -r;
-  for (int q = 0; q < nq_w; q++) {
-    const int half = q & 1;
-    int j0 = 0, j1 = 0;
-    uint32_t code = 0;
-    float ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    if (q < nq) {
-      int cy = S.iy + l, cz = S.iz + g;
-      bool ok = f_lo <= f_hi;
+  for (int q = 0; q < nrow_w; q++) {
+    int f_lo = 1, f_hi = 0, cy = 0, cz = 0;
+    bool ok = false;
+    if (q < nrow) {
+      cy = S.iy + l;
+      cz = S.iz + g;
+      ok = true;
       if (T.mode & M_PER_Y) cy += cy < 0 ? T.ny : (cy >= T.ny ? -T.ny : 0);
       else ok = ok && cy >= 0 && cy < T.ny;
       if (T.mode & M_PER_Z) cz += cz < 0 ? T.nz : (cz >= T.nz ? -T.nz : 0);
       else ok = ok && cz >= 0 && cz < T.nz;
+      float reach = cutx;
+      if (narrow) {  // y and z are relative to the own cell: the row spans [l wy, (l + 1) wy)
+        const float dy = l > 0 ? (float)l * wy - pi.y : (l < 0 ? pi.y - (float)(l + 1) * wy : 0.0f);
+        const float dz = g > 0 ? (float)g * wz - pi.z : (g < 0 ? pi.z - (float)(g + 1) * wz : 0.0f);
+        const float d2 = (dy > 0.0f ? dy * dy : 0.0f) + (dz > 0.0f ? dz * dz : 0.0f);
+        ok = ok && d2 < c2;
+        reach = sqrtf(fmaxf(c2 - d2, 0.0f));
+      }
+      f_lo = fb + (int)floorf((pi.x - reach) * sc - DS_XWIN_MARGIN);
+      f_hi = fb + (int)floorf((pi.x + reach) * sc + DS_XWIN_MARGIN);
+      f_lo = f_lo < fmin ? fmin : f_lo;
+      f_hi = f_hi > fmax ? fmax : f_hi;
+      ok = ok && f_lo <= f_hi;
+    }
+    const int bsplit = (f_hi >> (xl + DS_XB_LOG)) << (xl + DS_XB_LOG);  // first fine index of f_hi's block
+    const bool split = ok && bsplit > f_lo;
+    const int nhalf = __any_sync(FULL, split) ? 2 : 1;
+    for (int half = 0; half < nhalf; half++) {
+      int j0 = 0, j1 = 0;
+      uint32_t code = 0;
+      float ox = 0.0f, oy = 0.0f, oz = 0.0f;
       const int a0 = half == 0 ? f_lo : bsplit;
       const int a1 = half == 0 ? (split ? bsplit - 1 : f_hi) : (split ? f_hi : bsplit - 1);
       if (ok && a0 <= a1) {
@@ -505,26 +530,26 @@ __device__ __forceinline__ void ds_walk_rows(const TubeDesc &T, const Stencil &S
         oz = sh.z - pi.z;
         code = (uint32_t)o << DS_OFS32_SHIFT;
       }
-      if (half == 1 && ++g > r) {
-        g = -r;
-        ++l;
+      const int len_w = __reduce_max_sync(FULL, j1 - j0);
+      for (int p0 = 0; p0 < len_w; p0 += DS_RPIECE) {
+        if (__any_sync(FULL, n + DS_RPIECE > CAP)) flush();
+        bool pass[DS_RPIECE];
+#pragma unroll
+        for (int t = 0; t < DS_RPIECE; t++) {
+          const int j = j0 + p0 + t;
+          pass[t] = (j < j1) && screen(j, ox, oy, oz);  // j1 - j0 <= len_w
+        }
+#pragma unroll
+        for (int t = 0; t < DS_RPIECE; t++)
+          if (pass[t]) {
+            lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t - sb);
+            n++;
+          }
       }
     }
-    const int len_w = __reduce_max_sync(FULL, j1 - j0);
-    for (int p0 = 0; p0 < len_w; p0 += DS_RPIECE) {
-      if (__any_sync(FULL, n + DS_RPIECE > CAP)) flush();
-      bool pass[DS_RPIECE];
-#pragma unroll
-      for (int t = 0; t < DS_RPIECE; t++) {
-        const int j = j0 + p0 + t;
-        pass[t] = (j < j1) && screen(j, ox, oy, oz);  // j1 - j0 <= len_w
-      }
-#pragma unroll
-      for (int t = 0; t < DS_RPIECE; t++)
-        if (pass[t]) {
-          lst[n * DS_SWEEP_THREADS] = code | (uint32_t)(j0 + p0 + t - sb);
-          n++;
-        }
+    if (q < nrow && ++g > r) {
+      g = -r;
+      ++l;
     }
   }
   flush();
