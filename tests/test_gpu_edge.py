@@ -57,3 +57,20 @@ def test_ragged_batch_with_empty_and_tiny_tubes(precision):
                     assert np.array_equal(getattr(batched[t][s], f), getattr(O.species[s], f)), (t, s, f)
     # frozen tube: positions unchanged
     assert np.array_equal(batched[2][0].x, tubes[2][0].x)
+
+
+def test_species_beyond_the_list_entry_limit_is_refused_before_allocating():
+    """A list entry holds a slot in 24 bits on the FP32 path (25 on the FP64
+    path): a species of more particles is DS_ERR_UNSUPPORTED at the first step,
+    before any device memory is taken.  A 19.4M-gas tube, generated on the
+    device, so no host arrays either."""
+    from dustyshock3d_gb300 import _lib
+    spec = ic.DeviceIC.dusty_sod(dx_left=1 / 2400, Ly=0.05)
+    P, counts = spec.plan()
+    assert counts[0] > 2 ** 24
+    P.precision = "fp32"
+    with Solver(P) as S:
+        S.init_tube(0, spec)
+        with pytest.raises(_lib.DsError, match="DS_ERR_UNSUPPORTED"):
+            S.step(1)
+        assert S.memory_bytes() == 0
