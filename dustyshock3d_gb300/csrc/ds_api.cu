@@ -121,6 +121,7 @@ struct ds_ctx {
   cudaStream_t stream2 = nullptr;
   cudaEvent_t e_fork = nullptr, e_up = nullptr, e_dens = nullptr, e_force = nullptr, e_join = nullptr;
   cudaGraphExec_t hgraph[2] = {nullptr, nullptr};
+  int side_blocks = 0;  // grid of the transfers overlapped with the step
   // timing
   cudaEvent_t ev[DS_NPHASE + 1] = {};
   std::vector<cudaEvent_t> tev;
@@ -404,10 +405,9 @@ __global__ void k_inverse(const Chunk *chunks, const TubeDesc *tubes, const int 
 // segments without host arrays carried over slot for slot.  PART 0: x, y, z
 // and pid (what the cell keys read); PART 1: the other fields and Ind.
 template <int PART>
-__global__ void k_bound_in(const Chunk *chunks, const TubeDesc *tubes, const BoundSeg *bs, const int *inv,
-                           DevState src, DevState dst) {
+__device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *tubes, const BoundSeg *bs,
+                                               const int *inv, DevState src, DevState dst) {
   constexpr int F0 = PART == 0 ? 0 : 3, F1 = PART == 0 ? 3 : NF;
-  const Chunk ch = chunks[blockIdx.x];
   const int i = ch.begin + (int)threadIdx.x;
   if (i >= ch.end) return;
   const BoundSeg &B = bs[ch.tube * DS_MAXS + ch.species];
@@ -434,17 +434,21 @@ __global__ void k_bound_in(const Chunk *chunks, const TubeDesc *tubes, const Bou
   if (PART == 0) dst.pid[i] = p;
   else dst.ind[i] = k;
 }
+template <int PART>
+__global__ void k_bound_in(const Chunk *chunks, int nchunks, const TubeDesc *tubes, const BoundSeg *bs,
+                           const int *inv, DevState src, DevState dst) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) bound_in_chunk<PART>(chunks[c], tubes, bs, inv, src, dst);
+}
 
 // The bound fields a step has made final, back to the host in caller order:
 // PART 0 after the density sweeps (rho, p), 1 after the force sweep (ax, ay,
 // az, t_stop), 2 at the end (x, y, z, vx, vy, vz, e).
 template <int PART>
-__global__ void k_bound_out(const Chunk *chunks, const TubeDesc *tubes, const BoundSeg *bs, const int *inv,
-                            DevState st) {
+__device__ __forceinline__ void bound_out_chunk(const Chunk &ch, const TubeDesc *tubes, const BoundSeg *bs,
+                                                const int *inv, DevState st) {
   constexpr int NOUT = PART == 0 ? 2 : (PART == 1 ? 4 : 7);
   constexpr int fl0[2] = {FRHO, FP}, fl1[4] = {FAX, FAY, FAZ, FTS};
   constexpr int fl2[7] = {FX, FY, FZ, FVX, FVY, FVZ, FE};
-  const Chunk ch = chunks[blockIdx.x];
   const int i = ch.begin + (int)threadIdx.x;
   if (i >= ch.end) return;
   const BoundSeg &B = bs[ch.tube * DS_MAXS + ch.species];
@@ -466,6 +470,12 @@ __global__ void k_bound_out(const Chunk *chunks, const TubeDesc *tubes, const Bo
   }
 }
 
+template <int PART>
+__global__ void k_bound_out(const Chunk *chunks, int nchunks, const TubeDesc *tubes, const BoundSeg *bs,
+                            const int *inv, DevState st) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) bound_out_chunk<PART>(chunks[c], tubes, bs, inv, st);
+}
+
 void enqueue_bound_step(ds_ctx *c) {
   cudaStream_t s = c->stream, s2 = c->stream2;
   const int nch = (int)c->ch_all.size();
@@ -474,8 +484,12 @@ void enqueue_bound_step(ds_ctx *c) {
   k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, old.pid, c->inv);
   cudaEventRecord(c->e_fork, s);
   cudaStreamWaitEvent(s2, c->e_fork, 0);
-  k_bound_in<0><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, old, neu);
-  k_bound_in<1><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, old, neu);
+  // The second stream's transfers run on a small grid: the link needs few
+  // loads in flight, and a grid of every chunk would take all the SMs' slots
+  // from the sort and the sweeps they are meant to overlap.
+  const int nside = nch < c->side_blocks ? nch : c->side_blocks;
+  k_bound_in<0><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+  k_bound_in<1><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
   cudaEventRecord(c->e_up, s2);
   c->parity = P0 ^ 1;  // the caller-order state; the sort brings it back to P0
   ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, s);
@@ -484,10 +498,10 @@ void enqueue_bound_step(ds_ctx *c) {
   enqueue_physics(c, nullptr, c->e_dens, c->e_force);
   DevState st = c->buf[c->parity].view();
   cudaStreamWaitEvent(s2, c->e_dens, 0);
-  k_bound_out<0><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
+  k_bound_out<0><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, st);
   cudaStreamWaitEvent(s2, c->e_force, 0);
-  k_bound_out<1><<<nch, DS_CHUNK, 0, s2>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
-  k_bound_out<2><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->d_bound, c->inv, st);
+  k_bound_out<1><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, st);
+  k_bound_out<2><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, st);
   cudaEventRecord(c->e_join, s2);
   cudaStreamWaitEvent(s, c->e_join, 0);
 }
@@ -1383,6 +1397,12 @@ ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *f
   if (!c->inv) DA(c->inv, c->N ? c->N : 1);
   if (!c->d_bound) DA(c->d_bound, c->hbound.size());
   if (!c->stream2) {
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+#ifndef DS_SIDE_BLOCKS_PER_SM
+#define DS_SIDE_BLOCKS_PER_SM 1  // measured on the 1.44M tube: 1 beats 2 and 4
+#endif
+    c->side_blocks = (sms > 0 ? sms : 1) * DS_SIDE_BLOCKS_PER_SM;
     CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
     cudaEvent_t *evs[] = {&c->e_fork, &c->e_up, &c->e_dens, &c->e_force, &c->e_join};
     for (cudaEvent_t *e : evs) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
