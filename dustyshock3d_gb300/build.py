@@ -25,6 +25,7 @@ SOURCES = {
     "ds_sweep64.cu": ["-fmad=false"],
     "ds_sweep32.cu": [],
     "ds_ic.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "ds_inittxt.cu": [],
 }
 
 
