@@ -1228,6 +1228,28 @@ ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms)
   ds_status st = finalize(c);
   if (st != DS_OK) return st;
   CK(cudaSetDevice(c->device));
+  if (!phase_ms) {  // the steps as ds_step runs them: graph replays between two events
+    if (c->tev.size() < 2) {
+      for (int k = (int)c->tev.size(); k < 2; k++) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c->tev.push_back(e);
+      }
+    }
+    CK(cudaEventRecord(c->tev[0], c->stream));
+    for (int k = 0; k < nsteps; k++) {
+      st = capture_graph(c, c->parity);
+      if (st != DS_OK) return st;
+      CK(cudaGraphLaunch(c->graph[c->parity], c->stream));
+      c->parity ^= 1;
+    }
+    CK(cudaEventRecord(c->tev[1], c->stream));
+    CK(cudaEventSynchronize(c->tev[1]));
+    float tot = 0;
+    CK(cudaEventElapsedTime(&tot, c->tev[0], c->tev[1]));
+    if (total_ms) *total_ms = tot;
+    return check_flags(c);
+  }
   // one event set per step so that the steps run back to back with a single
   // synchronisation at the end
   const size_t need = (size_t)nsteps * (DS_NPHASE + 1);

@@ -127,10 +127,20 @@ class Solver:
         _lib.check(self.L, self.ctx, self.L.ds_step_host(self.ctx, int(n)), "ds_step_host")
 
     def step_timed(self, n: int = 1):
+        """(total ms, per-phase ms) of n steps with their kernels launched one by
+        one and events between phases (ds_step_timed)."""
         tot = ctypes.c_float(0)
         ph = (ctypes.c_float * _lib.DS_NPHASE)()
         _lib.check(self.L, self.ctx, self.L.ds_step_timed(self.ctx, int(n), ctypes.byref(tot), ph), "ds_step_timed")
         return tot.value, list(ph)
+
+    def step_timed_graph(self, n: int = 1) -> float:
+        """Device ms of n steps as ds_step runs them (graph replays between two
+        events; ds_step_timed with no phase split)."""
+        tot = ctypes.c_float(0)
+        _lib.check(self.L, self.ctx, self.L.ds_step_timed(self.ctx, int(n), ctypes.byref(tot), None),
+                   "ds_step_timed")
+        return tot.value
 
     # -- download -----------------------------------------------------------
     def get_species(self, tube: int, s: int, template: Species = None) -> Species:

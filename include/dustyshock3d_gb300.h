@@ -353,7 +353,9 @@ ds_status ds_load_tube(ds_ctx *c, int tube, const char *path);
  * device time and the per-phase sums in milliseconds: [0] keys, sort, reorder,
  * cell ranges, IDIC-key sort; [1] density sweeps with the EOS (and, on the
  * FP32 path, the force neighbour lists); [2] t_stop, step size, force sweep;
- * [3] IDIC reduce + solve, relax, move, energy. */
+ * [3] IDIC reduce + solve, relax, move, energy.  phase_ms may be NULL: then
+ * the steps are the captured graphs ds_step replays, between two events, and
+ * only the total is returned. */
 ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms);
 
 /* Number of kernels one step launches (the library's own kernels). */
