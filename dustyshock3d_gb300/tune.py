@@ -74,7 +74,7 @@ def tune(tubes: Sequence[Tuple[Params, List[Species]]], sample: int = 8, warmup:
             for t, (_, sp) in enumerate(sub):
                 S.set_tube(t, sp)
             S.step(warmup)
-            ms, _ = S.step_timed(steps)
+            ms = S.step_timed_graph(steps)  # as ds_step runs the batch: its captured graphs
         ms /= steps
         log.append((stencil, factor, depth, ms))
         if best is None or ms < best.ms_per_step:
