@@ -73,7 +73,9 @@ typedef enum ds_status {
 
 #define DS_PRECISION_FP64 0 /* FP64 everywhere, reference operation order */
 #define DS_PRECISION_FP32 1 /* FP32 neighbour sums (Kahan), cell-relative FP32
-                               positions; FP64 state, IDIC exchange, sums   */
+                               positions; FP64 state, IDIC exchange, sums.
+                               Needs DS_MODE_GRID_PROPER (else
+                               DS_ERR_UNSUPPORTED at ds_create)              */
 
 /* Run parameters: Init.txt lines 2-18 (kernel.cu:1707-1723), the constants the
  * reference hard-codes, and the extensions.  Fill with ds_params_init. */

@@ -416,3 +416,30 @@ def test_pinned_upload_download_equal_pageable(precision):
     finally:
         for p in keep:
             L.ds_host_free(p)
+
+
+@pytest.mark.parametrize("name", ["refB", "refC"])
+def test_fp32_path_with_reference_physics(name):
+    """The FP32 path needs the proper cell grid; with it, the reference's other
+    semantics (index-coupled t_stop, the species-1 eps guard, the 2-species
+    solve order, dust self-density every step) run on it.  After 10 steps it
+    is within the FP32 bound of the FP64 oracle on the same grid (relative L1
+    of gas rho <= 1e-5, velocities <= 1e-4 of their scale).  On the
+    reference's aliasing grid the FP32 path is refused."""
+    from dustyshock3d_gb300 import _lib
+    g, P, sp = setup(name)
+    bad = P.copy()
+    bad.precision = "fp32"
+    with pytest.raises(_lib.DsError, match="DS_ERR_UNSUPPORTED"):
+        Solver(bad)
+    P.mode = dataclasses.replace(P.mode, grid_proper=True)
+    P32 = P.copy()
+    P32.precision = "fp32"
+    gpu, _ = run_gpu(P32, sp, 10)
+    O = OracleState(P, sp).step(10)
+    gg, o = gpu[0], O.species[0]
+    assert np.abs(gg.rho - o.rho).sum() / np.abs(o.rho).sum() < 1e-5
+    vscale = np.abs(o.vx).max()
+    assert np.abs(gg.vx - o.vx).mean() / vscale < 1e-4
+    for k in (1, 2):
+        assert np.abs(gpu[k].vx - O.species[k].vx).mean() / max(np.abs(O.species[k].vx).max(), 1e-30) < 1e-4
