@@ -9,12 +9,14 @@ so no flush is needed between timed steps.
 
 Reported (one JSON line from rank 0):
   value      FP32 path (FP32 neighbour sums, Kahan; FP64 state, IDIC, sums),
-             device-resident, CUDA events around exactly --steps steps
+             device-resident, CUDA events around exactly --steps replays of
+             the step graphs ds_step runs (phases from a second pass)
   fp64       the plain FP64 path (reference operation order) on the same tube
   l1_*       L1 error of the FP32 path against the FP64 path after the run
-  e2e        the same metric through the C ABI with host buffers: every step
-             uploads the full particle state from pinned memory, steps once,
-             and downloads the full state
+  e2e        the same metric through the C ABI with host buffers: the pinned
+             host arrays are bound once (ds_bind_host) and each step
+             (ds_step_host) reads all of them and writes back what the step
+             changed; separate_calls: ds_upload_* + ds_step + ds_download_*
   roofline   the gas density sweep (dominant kernel): compulsory bytes / duration
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on a bounded sample
 
