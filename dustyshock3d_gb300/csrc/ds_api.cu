@@ -159,6 +159,20 @@ template <class T> ds_status dalloc(ds_ctx *c, T **p, size_t count) {
   return DS_OK;
 }
 
+// Temporary device buffers of one call, freed when the call returns, on an
+// early error return too (cudaFree waits for the device).
+struct ScratchDev {
+  std::vector<void *> held;
+  ~ScratchDev() {
+    for (void *q : held) cudaFree(q);
+  }
+  template <class T> cudaError_t alloc(T **out, size_t count) {
+    const cudaError_t e = cudaMalloc((void **)out, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) held.push_back(*out);
+    return e;
+  }
+};
+
 #define DA(ptr, count)                         \
   do {                                         \
     ds_status s_ = dalloc(c, &(ptr), (count)); \
@@ -1462,9 +1476,10 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
   if (ncand || nnb) {
     std::vector<Chunk> ch;
     add_chunks(ch, tube, species, b, b + n);
+    ScratchDev tmp;
     Chunk *d_ch = nullptr;
     if (!ch.empty()) {
-      CK(cudaMalloc(&d_ch, sizeof(Chunk) * ch.size()));
+      CK(tmp.alloc(&d_ch, ch.size()));
       CK(cudaMemcpyAsync(d_ch, ch.data(), sizeof(Chunk) * ch.size(), cudaMemcpyHostToDevice, c->stream));
       SweepArgs a = sweep_args(c, d_ch, (int)ch.size());
       ds_launch_counts64(a, (c->params[tube].mode & DS_MODE_H_PER_PARTICLE) != 0, c->any_proper, c->stream);
@@ -1473,13 +1488,13 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
     if (ncand && n) CK(cudaMemcpyAsync(ncand, c->ncand + b, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     if (nnb && n) CK(cudaMemcpyAsync(nnb, c->nnb + b, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (d_ch) CK(cudaFree(d_ch));
   }
   if (cell_key || head || next) {
+    ScratchDev tmp;
     int *dh = nullptr, *dn = nullptr, *dk = nullptr;
-    CK(cudaMalloc(&dh, sizeof(int) * (T.ncells + 1)));
-    CK(cudaMalloc(&dn, sizeof(int) * (n > 0 ? n : 1)));
-    CK(cudaMalloc(&dk, sizeof(int) * (n > 0 ? n : 1)));
+    CK(tmp.alloc(&dh, (size_t)T.ncells + 1));
+    CK(tmp.alloc(&dn, (size_t)n));
+    CK(tmp.alloc(&dk, (size_t)n));
     ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, 0, dh,
                           dn, dk, c->stream);
     CK(cudaGetLastError());
@@ -1487,7 +1502,6 @@ ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *h
     if (next && n) CK(cudaMemcpyAsync(next, dn, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     if (cell_key && n) CK(cudaMemcpyAsync(cell_key, dk, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(dh); cudaFree(dn); cudaFree(dk);
   }
   return DS_OK;
 }
@@ -1502,10 +1516,11 @@ ds_status ds_step_lists(ds_ctx *c, int tube, int species, int *head, int *next, 
   const int n = T.seg_end[species] - T.seg_begin[species];
   if (ncells) *ncells = T.ncells;
   if (!head && !next) return DS_OK;
+  ScratchDev tmp;
   int *dh = nullptr, *dn = nullptr, *dk = nullptr;
-  CK(cudaMalloc(&dh, sizeof(int) * (T.ncells + 1)));
-  CK(cudaMalloc(&dn, sizeof(int) * (n > 0 ? n : 1)));
-  CK(cudaMalloc(&dk, sizeof(int) * (n > 0 ? n : 1)));
+  CK(tmp.alloc(&dh, (size_t)T.ncells + 1));
+  CK(tmp.alloc(&dn, (size_t)n));
+  CK(tmp.alloc(&dk, (size_t)n));
   // the slots still hold the last sort's order (the step moves particles in place)
   ds_launch_debug_lists(c->d_tubes, tube, species, n, T.ncells, c->buf[c->parity].view(), c->cell_start, c->last_xl,
                         dh, dn, dk, c->stream);
@@ -1513,7 +1528,6 @@ ds_status ds_step_lists(ds_ctx *c, int tube, int species, int *head, int *next, 
   if (head) CK(cudaMemcpyAsync(head, dh, sizeof(int) * (T.ncells + 1), cudaMemcpyDeviceToHost, c->stream));
   if (next && n) CK(cudaMemcpyAsync(next, dn, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  cudaFree(dh); cudaFree(dn); cudaFree(dk);
   return DS_OK;
 }
 
