@@ -266,8 +266,8 @@ ds_status ds_synchronize(ds_ctx *c);
 
 /* Host arrays as the state of record, the way the reference's host keeps its
  * data.h arrays between steps and copies them to and from the GPU inside the
- * step (56 cudaMemcpy calls per step, e.g. kernel.cu:2026-2027, 2268-2270,
- * 2476-2482).  ds_bind_host binds caller-owned pinned arrays
+ * step (53 blocking cudaMemcpy calls in the step body, kernel.cu:1929-2527,
+ * e.g. 2026-2027, 2268-2270, 2476-2482).  ds_bind_host binds caller-owned pinned arrays
  * (ds_host_alloc, cudaMallocHost, or cudaHostRegister'ed) to one species of
  * one tube: fields[0..14] = x, y, z, vx, vy, vz, ax, ay, az, rho, p, e, mas,
  * h, t_stop as in ds_get_fields, n = the species' particle count, ind its Ind.
