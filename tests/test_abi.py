@@ -85,3 +85,17 @@ def test_checkpoint_params_reads_the_header_and_rejects_bad_files(tmp_path):
         f.write_bytes(data)
         assert L.ds_checkpoint_params(str(f).encode(), ctypes.byref(Q)) == 7, name
     assert L.ds_checkpoint_params(str(tmp_path / "missing").encode(), ctypes.byref(Q)) == 7
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    """No fallback: without the built library every entry point raises."""
+    import pytest
+    from dustyshock3d_gb300 import params
+    from dustyshock3d_gb300 import solver as solver_mod
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(_lib.DsError, match="not built"):
+        _lib.load(str(tmp_path / "libdustyshock3d_gb300.so"))
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libdustyshock3d_gb300.so"))
+    monkeypatch.setattr(_lib.load, "__defaults__", (str(tmp_path / "libdustyshock3d_gb300.so"),))
+    with pytest.raises(_lib.DsError):
+        solver_mod.Solver(params.Params())
