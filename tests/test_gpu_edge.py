@@ -74,3 +74,30 @@ def test_species_beyond_the_list_entry_limit_is_refused_before_allocating():
         with pytest.raises(_lib.DsError, match="DS_ERR_UNSUPPORTED"):
             S.step(1)
         assert S.memory_bytes() == 0
+
+
+def test_particle_outside_the_grid_flags_and_matches_the_oracle():
+    """A free gas particle outside the box: its neighbour key falls off the grid
+    (dropped from the lists, still moved: kernel.cu:1950) and its IDIC cell index
+    is out of range, where the reference writes out of bounds (kernel.cu:2116);
+    here the particle is left unrelaxed and DS_FLAG_IDIC_RANGE is raised, which
+    fails ds_step with DS_ERR_DEVICE.  The state equals the oracle's bit for bit."""
+    from dustyshock3d_gb300 import _lib
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25))
+    g = sp[0].copy().fill_missing()
+    free = np.nonzero(g.ind == 0)[0]
+    q = free[len(free) // 2]
+    g.x[q] = P.X_max + 0.25  # beyond the last IDIC cell (the grid has int(L / w) + 1 cells per axis)
+    species = [g, sp[1].copy().fill_missing()]
+    with Solver(P) as S:
+        S.set_tube(0, species)
+        with pytest.raises(_lib.DsError, match="DS_ERR_DEVICE"):
+            S.step(1)
+        assert S.device_flags() & 1
+        gpu = [S.get_species(0, s) for s in range(2)]
+    O = OracleState(P, species).step(1)
+    assert O.last_status & 1
+    for s in range(2):
+        for f in ("x", "y", "z", "vx", "vy", "vz", "rho"):
+            a, b = getattr(gpu[s], f), getattr(O.species[s], f)
+            assert np.array_equal(a, b, equal_nan=True), (s, f, np.nonzero(a != b)[0][:5])
