@@ -263,6 +263,21 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
     return fail(c, DS_ERR_UNSUPPORTED, "the fp32 path needs the proper cell grid (DS_MODE_GRID_PROPER)");
   if (((P.mode & (DS_MODE_PERIODIC_Y | DS_MODE_PERIODIC_Z)) != 0) && !(P.mode & DS_MODE_GRID_PROPER))
     return fail(c, DS_ERR_UNSUPPORTED, "periodic axes need the proper cell grid (DS_MODE_GRID_PROPER)");
+  {  // the grid sizes in double first: the int conversions and products of build_desc must not overflow
+    const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;
+    const double aw = P.idic_w > 0 ? P.idic_w : P.Coeff_h_dust_cell * P.h;
+    if (!(w > 0) || !(aw > 0) || !std::isfinite(w) || !std::isfinite(aw))
+      return fail(c, DS_ERR_ARG, "cell widths must be positive and finite");
+    const double ext[3] = {P.X_max - P.X_min, P.Y_max - P.Y_min, P.Z_max - P.Z_min};
+    double cells = 1.0, icells = 1.0;
+    for (double l : ext) {
+      if (!std::isfinite(l) || l < 0) return fail(c, DS_ERR_ARG, "box extent must be finite and positive");
+      cells *= std::floor(l / w) + 1.0;
+      icells *= std::floor(l / aw) + 1.0;
+    }
+    if (!(cells <= (double)(1 << 28))) return fail(c, DS_ERR_ARG, "neighbour grid too large");
+    if (!(icells <= (double)(1 << 28))) return fail(c, DS_ERR_ARG, "IDIC grid too large");
+  }
   TubeDesc T;
   build_desc(P, T);
   if (T.Cnx < 0 || T.Cny < 0 || T.Cnz < 0) return fail(c, DS_ERR_ARG, "box extent must be positive");

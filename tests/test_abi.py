@@ -99,3 +99,21 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(_lib.load, "__defaults__", (str(tmp_path / "libdustyshock3d_gb300.so"),))
     with pytest.raises(_lib.DsError):
         solver_mod.Solver(params.Params())
+
+
+def test_extreme_grids_are_refused_before_any_device_work():
+    """Box extents and cell widths are checked in double before the grid's int
+    sizes are formed: NaN or negative extents, zero widths and grids beyond 2^28
+    cells are DS_ERR_ARG from ds_create (no CUDA call is made before the check)."""
+    L = _lib.load()
+    base = _lib.DsParams()
+    assert L.ds_params_init(ctypes.byref(base)) == 0
+    cases = [dict(X_max=float("nan")), dict(X_max=-5.0), dict(cell_w=1e-9), dict(X_min=-1e12, X_max=1e12),
+             dict(idic_w=0.0, Coeff_h_dust_cell=0.0), dict(idic_w=1e-9)]
+    for kw in cases:
+        p = _lib.DsParams.from_buffer_copy(base)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        ctx = ctypes.c_void_p()
+        assert L.ds_create(ctypes.byref(p), ctypes.byref(ctx)) == 1, kw
+        assert not ctx.value
