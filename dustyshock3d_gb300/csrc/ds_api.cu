@@ -250,6 +250,7 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   const double wmin = fmin(T.wx, fmin(T.wy, T.wz));
   T.r1_hmax = T.stencil >= 2 ? 0.5 * wmin * (1.0 - 1e-9) : 1e300;
   T.rw = 1.0 / (wmin * (1.0 - 1e-9));
+  T.reach_hmax = proper ? 0.5 * T.stencil * wmin * (1.0 + 1e-9) : 1e300;
   T.inv_wx = 1.0 / T.wx; T.inv_wy = 1.0 / T.wy; T.inv_wz = 1.0 / T.wz; T.inv_aw = 1.0 / T.aw;
 }
 
@@ -355,7 +356,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorde
   const uint32_t *sval = alt ? c->valt : c->vin;
   if (before_reorder) cudaStreamWaitEvent(s, before_reorder, 0);  // fields still arriving from the host
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
-                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, fast, s);
+                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, c->d_flags, fast, s);
   ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s);
   c->skey = skey;
   if (c->any_stencil2)

@@ -100,7 +100,8 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
 template <bool FAST>
 __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                           const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32,
-                          int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid) {
+                          int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid,
+                          int *flags) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int q = ch.begin + threadIdx.x;
@@ -115,6 +116,9 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     dst.rho[q] = src.rho[j]; dst.p[q] = src.p[j]; dst.e[q] = src.e[j];
     const double m = src.m[j], h = src.h[j];
     dst.m[q] = m; dst.h[q] = h;
+    // proper grid: the cut-off 2h must stay within the stencil's cells, or the
+    // walks (ds_radius clamps to the stencil) would miss partners
+    if (!(((T.mode & M_HPP) ? h : T.h) <= T.reach_hmax)) atomicOr(flags, 8);  // DS_FLAG_REACH
     dst.ts[q] = src.ts[j];
     const int ind = src.ind[j], pid = src.pid[j];
     dst.ind[q] = ind; dst.pid[q] = pid;
@@ -643,14 +647,15 @@ void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, Dev
 }
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
-                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, bool fast, cudaStream_t s) {
+                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
+                       cudaStream_t s) {
   if (!nchunks) return;
   if (fast)
     k_reorder<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
-                                                 idic_local, ikin, ivin, slot_of_pid, ind_of_pid);
+                                                 idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags);
   else
     k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
-                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid);
+                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags);
 }
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s) {
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start);

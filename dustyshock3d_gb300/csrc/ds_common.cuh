@@ -56,6 +56,7 @@ struct TubeDesc {
   int stencil;       // cells searched on each side at most (FP64 path: 1 or 2; FP32 path: 1..4)
   int xl;            // FP32 path: sub-cell x bits of the sort keys (key = cell << xl | x bin)
   double r1_hmax;    // particles and cells with h <= r1_hmax need only the 27 inner cells
+  double reach_hmax; // proper grid: largest h whose cut-off 2h the stencil's cells cover
   double rw;         // 1 / (min cell width (1 - 1e-9)): a cut-off c needs ceil(c rw) cells per side
   double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
   // segments

@@ -27,7 +27,8 @@ void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, Dev
                     uint32_t *vin, bool fast, cudaStream_t s);
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
-                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, bool fast, cudaStream_t s);
+                       uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
+                       cudaStream_t s);
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s);
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,

@@ -245,7 +245,8 @@ class Solver:
     def device_flags(self) -> int:
         """Sticky device flags of the context (DS_FLAG_* bits of the ABI):
         1 IDIC index out of range, 2 dust index beyond the gas count,
-        4 a non-finite velocity, position or energy."""
+        4 a non-finite velocity, position or energy, 8 a cut-off beyond the
+        stencil's cells (proper grid)."""
         flags = ctypes.c_int(0)
         msg = ctypes.create_string_buffer(512)
         _lib.check(self.L, self.ctx, self.L.ds_last_error(self.ctx, ctypes.byref(flags), msg, 512), "ds_last_error")

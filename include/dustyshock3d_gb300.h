@@ -54,6 +54,14 @@ typedef enum ds_status {
                                   is undefined there; here the particle drops out
                                   of the cell lists).  The other flags make
                                   ds_step return DS_ERR_DEVICE.                 */
+#define DS_FLAG_REACH 0x8      /* proper cell grid only: a particle's cut-off 2h
+                                  reached past the cells the tube's stencil
+                                  covers (2h > stencil x the narrowest cell
+                                  width), so partners beyond them were missed.
+                                  Raise the stencil or the cell width.  (On
+                                  the reference grid the fixed 27 cells,
+                                  kernel.cu:2014-2016, drop such partners
+                                  silently, as the reference does.)            */
 
 /* Mode bits (ds_params.mode).  0 = the reference's own step. */
 #define DS_MODE_PERIODIC_Y 0x0001

@@ -383,6 +383,12 @@ int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken)
   const int hpp = (P->flags & ORC_H_PER_PARTICLE) != 0;
   const int coupled = (P->flags & ORC_REF_INDEX_COUPLING) != 0;
   int status = 0;
+  if (G.proper) { /* a cut-off 2h past the stencil's cells would miss partners: flag 8 */
+    const double reach = 0.5 * (P->stencil == 2 ? 2 : 1) * fmin(G.wx, fmin(G.wy, G.wz)) * (1.0 + 1e-9);
+    for (int s = 0; s < ns; s++)
+      for (int i = 0; i < sp[s].n; i++)
+        if (!((hpp ? sp[s].h[i] : P->h) <= reach)) status |= 8;
+  }
 
   /* lists for every species (kernel.cu:1937-1995) */
   int *head[1 + ORC_MAX_DUST], *next[1 + ORC_MAX_DUST];

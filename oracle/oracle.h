@@ -70,7 +70,10 @@ typedef struct orc_species {
 } orc_species;
 
 /* One time step of every species (sp[0] gas, sp[1..n_dust] dust).
- * *Tm is advanced by the step actually taken (returned in *dt_taken). */
+ * *Tm is advanced by the step actually taken (returned in *dt_taken).
+ * Returns -1 for a periodic axis too short for the stencil, else the flags
+ * of the library's DS_FLAG_* bits that the step raised: 1 IDIC index out of
+ * range, 8 a cut-off 2h past the stencil's cells on the proper grid. */
 int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken);
 
 /* Linked lists of one species exactly as the reference builds them

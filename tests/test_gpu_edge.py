@@ -101,3 +101,53 @@ def test_particle_outside_the_grid_flags_and_matches_the_oracle():
         for f in ("x", "y", "z", "vx", "vy", "vz", "rho"):
             a, b = getattr(gpu[s], f), getattr(O.species[s], f)
             assert np.array_equal(a, b, equal_nan=True), (s, f, np.nonzero(a != b)[0][:5])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_cutoff_beyond_the_stencil_is_flagged(precision):
+    """Proper cell grid, stencil 2 over cells of 1.001 h_max: a particle whose
+    cut-off 2h reaches past the two cells each side would lose partners (the
+    walks search the stencil's cells at most), so DS_FLAG_REACH is raised and
+    ds_step fails with DS_ERR_DEVICE.  h just inside the reach steps cleanly."""
+    from dustyshock3d_gb300 import _lib
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25))
+    P.precision = precision
+    assert P.stencil == 2
+    g = sp[0].copy().fill_missing()
+    free = np.nonzero(g.ind == 0)[0]
+    q = free[len(free) // 3]
+    for factor, flagged in ((0.999, False), (1.05, True)):
+        g2 = g.copy()
+        g2.h[q] = factor * P.cell_w  # reach = stencil x cell width / 2 = cell_w
+        with Solver(P) as S:
+            S.set_tube(0, [g2, sp[1].copy().fill_missing()])
+            if flagged:
+                with pytest.raises(_lib.DsError, match="DS_ERR_DEVICE"):
+                    S.step(1)
+                assert S.device_flags() & 8
+            else:
+                S.step(1)
+                assert S.device_flags() == 0
+
+
+def test_cutoff_beyond_the_cell_on_the_reference_grid_is_not_flagged():
+    """The reference grid searches its 27 cells of width 2h whatever a
+    particle's h field holds (kernel.cu:2014-2016): an oversize h there is the
+    reference's behaviour, not an error.  No flag, and the step equals the
+    oracle's bit for bit."""
+    from tests import _golden
+    _, P, sp = _golden.setup("refB")
+    assert not P.mode.grid_proper
+    g = sp[0].copy().fill_missing()
+    free = np.nonzero(g.ind == 0)[0]
+    g.h[free[len(free) // 2]] = 1.5 * P.h
+    species = [g] + [d.copy().fill_missing() for d in sp[1:]]
+    with Solver(P) as S:
+        S.set_tube(0, species)
+        S.step(1)
+        assert S.device_flags() & 8 == 0
+        gpu = [S.get_species(0, s) for s in range(len(species))]
+    O = OracleState(P, species).step(1)
+    for s in range(len(species)):
+        for f in ("x", "vx", "rho"):
+            assert np.array_equal(getattr(gpu[s], f), getattr(O.species[s], f), equal_nan=True), (s, f)

@@ -61,3 +61,24 @@ def test_idic_conserves_cell_momentum():
     vg, vd = 0.5, [0.1, -0.4, 0.9]
     g, d = orc.solve_cell(eps, t, vg, vd, 0.0, 5e-4)
     assert g + np.dot(eps, d) == pytest.approx(vg + np.dot(eps, vd), rel=1e-12)
+
+
+def test_step_flags_a_cutoff_past_the_stencil():
+    """Proper grid, stencil 2 over cells of 1.001 h_max: an h just inside the
+    reach (stencil x cell width / 2) raises nothing, one past it raises flag 8
+    (the library's DS_FLAG_REACH); the reference grid raises it for no h."""
+    from dustyshock3d_gb300 import ic
+    from tests import _golden
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25))
+    assert P.stencil == 2
+    q = int(np.nonzero(sp[0].ind == 0)[0][0])
+    for factor, want in ((0.999, 0), (1.05, 8)):
+        g = sp[0].copy().fill_missing()
+        g.h[q] = factor * P.cell_w
+        O = orc.OracleState(P, [g, sp[1].copy().fill_missing()]).step(1)
+        assert O.last_status & 8 == want, factor
+    _, R, rsp = _golden.setup("refB")
+    g = rsp[0].copy().fill_missing()
+    g.h[:] = 3.0 * R.h
+    O = orc.OracleState(R, [g] + [d.copy().fill_missing() for d in rsp[1:]]).step(1)
+    assert O.last_status & 8 == 0
