@@ -568,7 +568,8 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
 // largest h within the tube's stencil (ds_radius), so cells whose cut-offs are
 // short walk fewer cells.  Separable passes over the key space: h_max per cell,
 // its maximum over the x window, the y window, then the z window (periodic
-// axes wrap).  Reference grids and the orphan buckets keep the tube's stencil.
+// axes wrap).  Reference grids and the orphan buckets keep the tube's stencil;
+// tubes without per-particle h (every cut-off 2 h of the run) take its radius.
 __global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const double *h, double *hmax) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
@@ -592,6 +593,10 @@ __global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const
   if (whole) {
     if (AXIS == 2) krad[key] = (unsigned char)T.stencil;
     else out[key] = in[key];
+    return;
+  }
+  if (!(T.mode & M_HPP)) {  // one h for every pair (the run's h, not the h field): one radius
+    if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * T.h);
     return;
   }
   const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);

@@ -82,3 +82,19 @@ def test_step_flags_a_cutoff_past_the_stencil():
     g.h[:] = 3.0 * R.h
     O = orc.OracleState(R, [g] + [d.copy().fill_missing() for d in rsp[1:]]).step(1)
     assert O.last_status & 8 == 0
+
+
+def test_split_species_moves_the_gas_as_one():
+    """Three dust species on the same sites with one stopping time and mass
+    ratios summing to 1 drag the gas as one species of ratio 1 does: with
+    equal t_k the implicit solve sees the species only through sum_k eps_k."""
+    from tests._multidust import multi_dust_tube
+    P1, sp1 = multi_dust_tube((1.0,), (2e-3,), shift=False)
+    P3, sp3 = multi_dust_tube((0.2, 0.3, 0.5), (2e-3,) * 3, shift=False)
+    A = orc.OracleState(P1, sp1).step(4)
+    B = orc.OracleState(P3, sp3).step(4)
+    for f in ("x", "vx", "rho", "e"):
+        a, b = getattr(A.species[0], f), getattr(B.species[0], f)
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), f
+    for k in (1, 2, 3):
+        assert np.abs(B.species[k].vx - A.species[1].vx).max() <= 1e-12 * np.abs(A.species[1].vx).max(), k
