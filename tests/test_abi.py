@@ -117,3 +117,23 @@ def test_extreme_grids_are_refused_before_any_device_work():
         ctx = ctypes.c_void_p()
         assert L.ds_create(ctypes.byref(p), ctypes.byref(ctx)) == 1, kw
         assert not ctx.value
+
+
+def test_unsupported_combinations_are_refused_before_any_device_work():
+    """Combinations the step does not implement are DS_ERR_UNSUPPORTED from
+    ds_create: periodic axes or the FP32 path on the reference's aliasing grid
+    (its rows are not true rows), wide stencils without the proper grid, and
+    stencils past 2 cells on the FP64 path."""
+    L = _lib.load()
+    base = _lib.DsParams()
+    assert L.ds_params_init(ctypes.byref(base)) == 0
+    proper = 0x0400
+    cases = [dict(mode=0x0001), dict(mode=0x0002), dict(precision=1), dict(stencil=2),
+             dict(stencil=3, mode=proper)]
+    for kw in cases:
+        p = _lib.DsParams.from_buffer_copy(base)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        ctx = ctypes.c_void_p()
+        assert L.ds_create(ctypes.byref(p), ctypes.byref(ctx)) == 6, kw
+        assert not ctx.value

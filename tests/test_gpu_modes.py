@@ -3,7 +3,8 @@
 The benchmark physics (Mode.baseline()) and the reference's own step
 (Mode.reference()) are covered by the parity tests; here each switch of the
 mode word, and the isothermal equation of state (Type_of_state 1,
-kernel.cu:95-96), is flipped alone from the benchmark physics.  Every variant:
+kernel.cu:95-96), is flipped alone from the benchmark physics and from the
+reference's step.  Every variant from the benchmark physics:
 the FP64 path equals the oracle bit for bit after 4 steps, and the FP32 path
 tracks the oracle within the parity tests' FP32 tolerance after 10."""
 import numpy as np
@@ -71,3 +72,51 @@ def test_switch_fp32_tracks_the_oracle(name):
     assert np.abs(g.vx - o.vx).mean() / vscale < 1e-4
     for k in range(1, len(sp)):
         assert np.abs(gpu[k].vx - O.species[k].vx).mean() / vscale < 1e-4, k
+
+
+REF_SWITCHES = ["h_per_particle", "tstop_const", "gas_accel_particle", "ref_index_coupling",
+                "ref_eps_guard", "ref_solve2", "cfl", "dust_rho", "grid_proper", "idic_proper", "isothermal"]
+
+
+@pytest.mark.parametrize("name", REF_SWITCHES)
+def test_reference_step_with_one_switch_fp64_bitexact(name):
+    """The same from the reference's own step (case refB: gas and two dust
+    species on the reference's aliasing grid): every switch flipped alone,
+    FP64 path = oracle bit for bit after 5 steps.  (Periodic axes need the
+    proper grid: refused at ds_create on this one.)"""
+    from tests import _golden
+    _, P, sp = _golden.setup("refB")
+    P = P.copy()
+    m = P.mode
+    if name == "isothermal":
+        P.Type_of_state = 1
+    elif name == "tstop_const":
+        m.tstop_const = True
+        P.t_stop_const = [1e-3, 1e-2]
+    elif name == "cfl":
+        m.cfl = True
+        P.cfl = 0.3
+    else:
+        setattr(m, name, not getattr(m, name))
+    gpu, (Tm, dt, _) = run_gpu(P, sp, 5)
+    O = OracleState(P, sp).step(5)
+    assert O.last_status == 0
+    assert Tm == O.Tm and dt == O.last_dt
+    compare_exact(gpu, O.species, name)
+
+
+@pytest.mark.parametrize("stencil,cell_factor", [(3, 0.6673), (4, 0.5005)])
+def test_one_h_with_small_cells_fp32(stencil, cell_factor):
+    """One h for every pair on cells of h / 1.5 and h / 2 (3 and 4 cells each
+    side): the FP32 path tracks the oracle on its own grid."""
+    P, sp = _flip("h_per_particle")
+    P32 = P.copy()
+    P32.precision = "fp32"
+    P32.stencil = stencil
+    P32.cell_w = cell_factor * P.h
+    gpu, _ = run_gpu(P32, sp, 10)
+    O = OracleState(P, sp).step(10)
+    g, o = gpu[0], O.species[0]
+    assert np.abs(g.rho - o.rho).sum() / np.abs(o.rho).sum() < 1e-5
+    vscale = np.abs(o.vx).max()
+    assert np.abs(g.vx - o.vx).mean() / vscale < 1e-4
