@@ -151,3 +151,19 @@ def test_cutoff_beyond_the_cell_on_the_reference_grid_is_not_flagged():
     for s in range(len(species)):
         for f in ("x", "vx", "rho"):
             assert np.array_equal(getattr(gpu[s], f), getattr(O.species[s], f), equal_nan=True), (s, f)
+
+
+def test_lattice_on_the_cell_faces_fp64_bitexact():
+    """Gas and dust lattices starting exactly on the faces of the IDIC cells
+    (a quarter of the gas sits on an x face): the cell of such a particle is
+    decided by the rounding of (x - origin) / width, done as the oracle does it,
+    so the FP64 path still equals the oracle bit for bit after 6 steps."""
+    from tests.test_gpu_parity import compare_exact, run_gpu
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25),
+                              lattice_offset=0.0)
+    fx = (sp[0].x - P.X_min) / P.idic_w
+    assert np.sum(np.abs(fx - np.round(fx)) < 1e-12) > sp[0].n // 8
+    gpu, (Tm, dt, _) = run_gpu(P, sp, 6)
+    O = OracleState(P, sp).step(6)
+    assert Tm == O.Tm and dt == O.last_dt
+    compare_exact(gpu, O.species, "lattice on the faces")
