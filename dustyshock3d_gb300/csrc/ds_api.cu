@@ -93,6 +93,7 @@ struct ds_ctx {
   int *d_nseg_key0 = nullptr, *d_nseg_tube = nullptr, *d_nseg_species = nullptr;
   double *cwa = nullptr, *cwb = nullptr;  // stencil-radius passes (h maxima per key)
   unsigned char *krad = nullptr;
+  double *origins = nullptr;  // FP32 path: TubeDesc::orig of every tube
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
@@ -185,6 +186,18 @@ int bits_for(long long n) {
   return b;
 }
 
+// FP32 path index maps (TubeDesc::kxa ...) for the tube's x bits xl: scaling
+// by 2^xl is exact, so the fine x index's top bits are the x cell.
+void set_index_maps(TubeDesc &T) {
+  T.kxa = std::ldexp(T.inv_wx, T.xl); T.kxb = -T.ox * T.kxa;
+  T.kya = T.inv_wy; T.kyb = -T.oy * T.inv_wy;
+  T.kza = T.inv_wz; T.kzb = -T.oz * T.inv_wz;
+  T.iaa = T.inv_aw;
+  T.iab[0] = -T.ox * T.inv_aw; T.iab[1] = -T.oy * T.inv_aw; T.iab[2] = -T.oz * T.inv_aw;
+  T.wrap_key[0] = ds_order_key(T.oy); T.wrap_key[1] = ds_order_key(T.ymax);
+  T.wrap_key[2] = ds_order_key(T.oz); T.wrap_key[3] = ds_order_key(T.zmax);
+}
+
 // Tube constants from its parameters; grid sizes follow kernel.cu:1767-1778
 // and kernel.cu:1577-1582 with the same arithmetic.
 void build_desc(const ds_params &P, TubeDesc &T) {
@@ -252,6 +265,7 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   T.rw = 1.0 / (wmin * (1.0 - 1e-9));
   T.reach_hmax = proper ? 0.5 * T.stencil * wmin * (1.0 + 1e-9) : 1e300;
   T.inv_wx = 1.0 / T.wx; T.inv_wy = 1.0 / T.wy; T.inv_wz = 1.0 / T.wz; T.inv_aw = 1.0 / T.aw;
+  set_index_maps(T);
 }
 
 ds_status check_params(ds_ctx *c, const ds_params &P) {
@@ -599,7 +613,10 @@ ds_status finalize(ds_ctx *c) {
     c->xl = DS_XL_MAX;
     while (c->xl > 0 && ((nkeys << c->xl) > 8LL * N + 4096 || c->key_bits + c->xl > 31)) c->xl--;
   }
-  for (auto &T : c->tdesc) T.xl = c->xl;
+  for (auto &T : c->tdesc) {
+    T.xl = c->xl;
+    set_index_maps(T);
+  }
   c->nikeys = (int)nikeys;
   c->ikey_bits = bits_for(nikeys);
   c->ncell_total = (int)ncell;
@@ -641,6 +658,23 @@ ds_status finalize(ds_ctx *c) {
   for (double **p : cd) CK(cudaMemsetAsync(*p, 0, sizeof(double) * (size_t)nikeys, c->stream));
   CK(cudaMemsetAsync(c->edot, 0, sizeof(double) * (size_t)(N ? N : 1), c->stream));
   CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+  // FP32 path: FP64 origins of every tube's x-blocks and y, z cells
+  if (c->any_fp32) {
+    size_t norig = 0;
+    for (auto &T : c->tdesc) {
+      T.nbx = (T.nx + DS_XB - 1) / DS_XB;
+      norig += (size_t)T.nbx + T.ny + T.nz;
+    }
+    DA(c->origins, norig);
+    size_t o = 0;
+    for (auto &T : c->tdesc) {
+      double *d = c->origins + o;
+      T.orig = d;
+      ds_launch_origins(T, d, c->stream);
+      o += (size_t)T.nbx + T.ny + T.nz;
+    }
+    CK(cudaGetLastError());
+  }
   // tables
   ds_status st;
   if ((st = upload_vec(c, &c->d_tubes, c->tdesc)) != DS_OK) return st;

@@ -30,6 +30,11 @@ __device__ __forceinline__ unsigned long long dbl_bits(double v) {
   return (unsigned long long)__double_as_longlong(v);
 }
 
+// isfinite on the exponent bits (integer pipe; the same answer as isfinite)
+__device__ __forceinline__ bool finite_bits(double v) {
+  return ((unsigned)__double2hiint(v) & 0x7ff00000u) != 0x7ff00000u;
+}
+
 __global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntubes) return;
@@ -38,14 +43,13 @@ __global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
   ts[t].dt = 0.0;
 }
 
-// Per-axis cell of a position in the proper grid, FP32 path: reciprocal
-// multiplies instead of FP64 divisions (GB300's FP64 divide is ~20x an FP32
-// multiply-add); periodic axes clamped.  Every cell index of the FP32 path
-// comes from here or from the sorted keys, so they are consistent.
+// IDIC cell of a position, FP32 path: one FMA and one rounding conversion per
+// axis (the index maps) instead of an FP64 division; GB300 runs FP64 at 2 lanes
+// per SM per clock, so these per-particle kernels are bound by that pipe.
 __device__ __forceinline__ int fast_idic_cell(const TubeDesc &T, double x, double y, double z) {
-  const int ix = (int)floor((x - T.ox) * T.inv_aw);
-  const int iy = (int)floor((y - T.oy) * T.inv_aw);
-  const int iz = (int)floor((z - T.oz) * T.inv_aw);
+  const int ix = __double2int_rd(fma(x, T.iaa, T.iab[0]));
+  const int iy = __double2int_rd(fma(y, T.iaa, T.iab[1]));
+  const int iz = __double2int_rd(fma(z, T.iaa, T.iab[2]));
   if (ix < 0 || ix >= T.anx || iy < 0 || iy >= T.any_ || iz < 0 || iz >= T.anz) return -1;
   const int c = ix + iy * T.asy + iz * T.asz;
   return (c < 0 || c > T.n_idic) ? -1 : c;
@@ -73,12 +77,8 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
       local = in ? ix + iy * T.sy + iz * T.sz : T.ncells + 1;
       // FP32 path: the particle's x within its cell in 2^xl bins, below the
       // cell in the key, so that each cell -- and so each row of cells -- is
-      // sorted by x
-      if (in) {
-        const double fx = (st.x[i] - T.ox) * T.inv_wx - (double)ix;
-        const int b = (int)(fx * (double)(1 << T.xl));
-        bin = (uint32_t)(b < 0 ? 0 : (b >= (1 << T.xl) ? (1 << T.xl) - 1 : b));
-      }
+      // sorted by x (the low bits of the fine x index)
+      if (in) bin = (uint32_t)ds_fast_fine_x(T, st.x[i]) & ((1u << T.xl) - 1u);
     } else {
       const int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
       if (!(T.mode & M_GRID_PROPER))
@@ -117,8 +117,10 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     const double m = src.m[j], h = src.h[j];
     dst.m[q] = m; dst.h[q] = h;
     // proper grid: the cut-off 2h must stay within the stencil's cells, or the
-    // walks (ds_radius clamps to the stencil) would miss partners
-    if (!(((T.mode & M_HPP) ? h : T.h) <= T.reach_hmax)) atomicOr(flags, 8);  // DS_FLAG_REACH
+    // walks (ds_radius clamps to the stencil) would miss partners.  Compared as
+    // bit patterns (integer pipe): h in [+0, reach] passes; NaN, negative h
+    // and h beyond the reach are flagged.
+    if (dbl_bits((T.mode & M_HPP) ? h : T.h) > dbl_bits(T.reach_hmax)) atomicOr(flags, 8);  // DS_FLAG_REACH
     dst.ts[q] = src.ts[j];
     const int ind = src.ind[j], pid = src.pid[j];
     dst.ind[q] = ind; dst.pid[q] = pid;
@@ -140,19 +142,28 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
       } else {
         ds_proper_cell(T, x, y, z, ix, iy, iz);
       }
-      // FP32 path: x relative to the x-block origin (row walks), y, z to the cell's
+      // FP32 path: x relative to the x-block origin (row walks), y, z to the
+      // cell's; the origins of grid cells from the tube's table (the same FP64
+      // values, without the FP64 multiply-adds)
       const int bx = FAST ? ((ix >> DS_XB_LOG) << DS_XB_LOG) : ix;
-      p4.x = (float)(x - (T.ox + bx * T.wx));
-      p4.y = (float)(y - (T.oy + iy * T.wy));
-      p4.z = (float)(z - (T.oz + iz * T.wz));
+      if (FAST && local < T.ncells) {
+        p4.x = ds_d2f(x - T.orig[ix >> DS_XB_LOG]);
+        p4.y = ds_d2f(y - T.orig[T.nbx + iy]);
+        p4.z = ds_d2f(z - T.orig[T.nbx + T.ny + iz]);
+      } else {
+        p4.x = ds_d2f(x - (T.ox + bx * T.wx));
+        p4.y = ds_d2f(y - (T.oy + iy * T.wy));
+        p4.z = ds_d2f(z - (T.oz + iz * T.wz));
+      }
     } else {
-      p4.x = (float)(x - T.fx);
-      p4.y = (float)(y - T.fy);
-      p4.z = (float)(z - T.fz);
+      p4.x = ds_d2f(x - T.fx);
+      p4.y = ds_d2f(y - T.fy);
+      p4.z = ds_d2f(z - T.fz);
     }
-    p4.w = (float)h;
+    // FP32 copies converted on the integer pipe (ds_d2f: the IEEE conversion)
+    p4.w = ds_d2f(h);
     pos32[q] = p4;
-    vm32[q] = make_float4((float)vx, (float)vy, (float)vz, (float)m);
+    vm32[q] = make_float4(ds_d2f(vx), ds_d2f(vy), ds_d2f(vz), ds_d2f(m));
     const int ic = FAST ? fast_idic_cell(T, x, y, z) : ds_idic_cell(T, x, y, z);
     idic_local[q] = ic;
     const int idst = FAST ? q : gp;
@@ -289,11 +300,104 @@ __device__ __forceinline__ void solve_comp(const double (&eps)[ND], const double
   for (int k = 0; k < ND; k++) d_out[k] = g - xn[k];
 }
 
+// FP32 path: the same per-cell solve (means, eps, Psi, the implicit drag and
+// the relax coefficients) with every quantity that does not depend on the
+// component computed once per cell and reciprocals in place of divisions:
+// ~8 FP64 divisions per cell instead of ~28 (GB300's FP64 pipe runs 2 lanes
+// per SM per clock).  With 1/b_k = eps_k tau / (t_k + tau) the
+// Sherman-Morrison terms of solve_comp reduce to
+//   xn_k = t_k / (t_k + tau) (r_k - S / beta),  S = sum_k r_k / b_k,
+// and a species with eps_k = 0 gives NaN there as solve_comp does.
+template <int ND>
+__device__ __forceinline__ void idic_solve_cell_fast(const TubeDesc &T, int c, double tau, CellArrays &ca) {
+  const int kg = T.idic_base[0] + c;
+  const int cg = ca.cnt[kg];
+  const double icg = cg > 0 ? 1.0 / cg : 0.0;
+  double vg[3] = {0.0, 0.0, 0.0}, ps[3] = {0.0, 0.0, 0.0};
+  if (cg > 0) {
+    vg[0] = ca.vx[kg] * icg; vg[1] = ca.vy[kg] * icg; vg[2] = ca.vz[kg] * icg;
+    ps[0] = ca.a0[kg] * icg; ps[1] = ca.a1[kg] * icg; ps[2] = ca.a2[kg] * icg;
+  }
+  double eps[ND], tt[ND], vd[3][ND], q[ND], q0[ND], ib[ND];
+  double beta = 1.0, E = 1.0;
+  const int c1 = ca.cnt[T.idic_base[1] + c];
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    const int kd = T.idic_base[k + 1] + c;
+    const int cd = ca.cnt[kd];
+    if (cd > 0) {
+      const double icd = 1.0 / cd;
+      vd[0][k] = ca.vx[kd] * icd; vd[1][k] = ca.vy[kd] * icd; vd[2][k] = ca.vz[kd] * icd;
+      tt[k] = ca.a0[kd] * icd;
+    } else {
+      vd[0][k] = 0.0; vd[1][k] = 0.0; vd[2][k] = 0.0;
+      tt[k] = T.t_empty;
+    }
+    const int guard = (T.mode & M_REF_EPS_GUARD) ? c1 : cd;
+    eps[k] = ((cg > 0) && (guard > 0)) ? (cd * T.mass_ratio[k]) * icg : T.eps_empty[k];
+    q[k] = 1.0 / (tt[k] + tau);
+    q0[k] = tt[k] * q[k];
+    ib[k] = eps[k] * tau * q[k];
+    beta = beta + ib[k];
+    E = E + eps[k];
+  }
+  const double ibeta = 1.0 / beta, iE = 1.0 / E;
+  double gnew[3], dnew[3][ND];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double tp = tau * ps[a];
+    double y = vg[a], S = 0.0, r[ND];
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+      y = fma(eps[k], vd[a][k], y);
+      r[k] = (vg[a] - vd[a][k]) + tp;
+      S = fma(r[k], ib[k], S);
+    }
+    const double Sb = S * ibeta;
+    double g = y + tp, xn[ND];
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+      xn[k] = eps[k] != 0.0 ? (r[k] - Sb) * q0[k] : __longlong_as_double(0x7ff8000000000000LL);
+      g = fma(eps[k], xn[k], g);
+    }
+    g = g * iE;
+    gnew[a] = g;
+#pragma unroll
+    for (int k = 0; k < ND; k++) dnew[a][k] = g - xn[k];
+  }
+  ca.nvx[kg] = gnew[0]; ca.nvy[kg] = gnew[1]; ca.nvz[kg] = gnew[2];
+  ca.px[kg] = ps[0]; ca.py[kg] = ps[1]; ca.pz[kg] = ps[2];
+  // relax coefficients (the relaxations of IDIC.h:276-313 as v_new = q0 v + q1 (...)):
+  //   dust  t/(t+tau) v + tau/(t+tau) g;  gas  (v/tau + N + a)/D, D = 1/tau + sum eps/t
+  const double itau = 1.0 / tau;
+  double D = itau, Nx = 0.0, Ny = 0.0, Nz = 0.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    const int kd = T.idic_base[k + 1] + c;
+    ca.nvx[kd] = dnew[0][k]; ca.nvy[kd] = dnew[1][k]; ca.nvz[kd] = dnew[2][k];
+    ca.px[kd] = tt[k];   // dust: mean t_stop
+    ca.py[kd] = eps[k];  // dust: eps
+    const double w = eps[k] / tt[k];
+    D = D + w;
+    Nx = fma(w, dnew[0][k], Nx); Ny = fma(w, dnew[1][k], Ny); Nz = fma(w, dnew[2][k], Nz);
+    ca.q0[kd] = q0[k];
+    ca.q1[kd] = tau * q[k];
+  }
+  const double iD = 1.0 / D;
+  ca.q0[kg] = iD * itau;
+  ca.q1[kg] = iD;
+  ca.a0[kg] = Nx; ca.a1[kg] = Ny; ca.a2[kg] = Nz;
+}
+
 // Per (tube, IDIC cell): means (kernel.cu:2126-2190), eps (2192-2211),
 // Psi (2302-2309), solve (2310-2437).  Results are written at the cell's key
 // of each species: new velocities; for gas Psi; for dust the mean t_stop and eps.
 template <int ND, bool FAST>
 __device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double tau, CellArrays &ca) {
+  if (FAST) {
+    idic_solve_cell_fast<ND>(T, c, tau, ca);
+    return;
+  }
   const int kg = T.idic_base[0] + c;
   const int cg = ca.cnt[kg];
   double vgx = 0.0, vgy = 0.0, vgz = 0.0, psx = 0.0, psy = 0.0, psz = 0.0;
@@ -330,25 +434,6 @@ __device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double
     ca.nvx[kd] = ox[k]; ca.nvy[kd] = oy[k]; ca.nvz[kd] = oz[k];
     ca.px[kd] = tt[k];   // dust: mean t_stop
     ca.py[kd] = eps[k];  // dust: eps
-  }
-  if (FAST) {
-    // The relaxations of IDIC.h:276-313 rewritten as v_new = q0 v + q1 (...),
-    // coefficients per cell in FP64, so a particle needs no division:
-    //   dust  (v/tau + g/t)/(1/tau + 1/t) = t/(t+tau) v + tau/(t+tau) g
-    //   gas   (v/tau + N + a)/D, D = 1/tau + sum eps/t, N = sum eps v_k/t
-    double D = 1.0 / tau, Nx = 0.0, Ny = 0.0, Nz = 0.0;
-#pragma unroll
-    for (int k = 0; k < ND; k++) {
-      const int kd = T.idic_base[k + 1] + c;
-      const double w = eps[k] / tt[k];
-      D = D + w;
-      Nx = Nx + w * ox[k]; Ny = Ny + w * oy[k]; Nz = Nz + w * oz[k];
-      ca.q0[kd] = tt[k] / (tt[k] + tau);
-      ca.q1[kd] = tau / (tt[k] + tau);
-    }
-    ca.q0[kg] = 1.0 / (tau * D);
-    ca.q1[kg] = 1.0 / D;
-    ca.a0[kg] = Nx; ca.a1[kg] = Ny; ca.a2[kg] = Nz;
   }
 }
 
@@ -395,18 +480,19 @@ __global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, con
       atomicOr(flags, 1);  // DS_FLAG_IDIC_RANGE: left unrelaxed
     } else if (FAST) {
       const int kg = T.idic_base[0] + cell;
+      // FP32 path: fused multiply-adds (fewer FP64-pipe instructions)
       if (s > 0) {
         const int kd = T.idic_base[s] + cell;
         const double a0 = ca.q0[kd], a1 = ca.q1[kd];
-        vx = a0 * vx + a1 * ca.nvx[kg];
-        vy = a0 * vy + a1 * ca.nvy[kg];
-        vz = a0 * vz + a1 * ca.nvz[kg];
+        vx = fma(a1, ca.nvx[kg], a0 * vx);
+        vy = fma(a1, ca.nvy[kg], a0 * vy);
+        vz = fma(a1, ca.nvz[kg], a0 * vz);
       } else {
         const bool own = (T.mode & M_GAS_ACC_P) != 0;
         const double a0 = ca.q0[kg], a1 = ca.q1[kg];
-        vx = a0 * vx + a1 * (ca.a0[kg] + (own ? st.ax[i] : ca.px[kg]));
-        vy = a0 * vy + a1 * (ca.a1[kg] + (own ? st.ay[i] : ca.py[kg]));
-        vz = a0 * vz + a1 * (ca.a2[kg] + (own ? st.az[i] : ca.pz[kg]));
+        vx = fma(a1, ca.a0[kg] + (own ? st.ax[i] : ca.px[kg]), a0 * vx);
+        vy = fma(a1, ca.a1[kg] + (own ? st.ay[i] : ca.py[kg]), a0 * vy);
+        vz = fma(a1, ca.a2[kg] + (own ? st.az[i] : ca.pz[kg]), a0 * vz);
       }
     } else if (s > 0) {
       const int kg = T.idic_base[0] + cell, kd = T.idic_base[s] + cell;
@@ -442,24 +528,38 @@ __global__ void k_relax_move(const TubeDesc *tubes, const TubeState *tstate, con
       vz = (vz / tau + tmp_z + az) / (1.0 / tau + tmp1);
     }
     st.vx[i] = vx; st.vy[i] = vy; st.vz[i] = vz;
-    double x = st.x[i] + vx * tau;
-    double y = st.y[i] + vy * tau;
-    double z = st.z[i] + vz * tau;
-    if (T.mode & M_PER_Y) {
-      if (y < T.oy) y = y + T.Ly;
-      else if (y >= T.ymax) y = y - T.Ly;
-    }
-    if (T.mode & M_PER_Z) {
-      if (z < T.oz) z = z + T.Lz;
-      else if (z >= T.zmax) z = z - T.Lz;
+    double x = FAST ? fma(vx, tau, st.x[i]) : st.x[i] + vx * tau;
+    double y = FAST ? fma(vy, tau, st.y[i]) : st.y[i] + vy * tau;
+    double z = FAST ? fma(vz, tau, st.z[i]) : st.z[i] + vz * tau;
+    if (FAST) {  // the same comparisons on order keys (integer pipe)
+      if (T.mode & M_PER_Y) {
+        const int64_t k = ds_order_key(y);
+        if (k < T.wrap_key[0]) y = y + T.Ly;
+        else if (k >= T.wrap_key[1]) y = y - T.Ly;
+      }
+      if (T.mode & M_PER_Z) {
+        const int64_t k = ds_order_key(z);
+        if (k < T.wrap_key[2]) z = z + T.Lz;
+        else if (k >= T.wrap_key[3]) z = z - T.Lz;
+      }
+    } else {
+      if (T.mode & M_PER_Y) {
+        if (y < T.oy) y = y + T.Ly;
+        else if (y >= T.ymax) y = y - T.Ly;
+      }
+      if (T.mode & M_PER_Z) {
+        if (z < T.oz) z = z + T.Lz;
+        else if (z >= T.zmax) z = z - T.Lz;
+      }
     }
     st.x[i] = x; st.y[i] = y; st.z[i] = z;
     double e = 0.0;
     if (s == 0) {
-      e = st.e[i] + edot[i] * tau;
+      e = FAST ? fma(edot[i], tau, st.e[i]) : st.e[i] + edot[i] * tau;
       st.e[i] = e;
     }
-    if (!(isfinite(vx) && isfinite(vy) && isfinite(vz) && isfinite(x) && isfinite(y) && isfinite(z) && isfinite(e)))
+    if (!(finite_bits(vx) && finite_bits(vy) && finite_bits(vz) && finite_bits(x) && finite_bits(y) &&
+          finite_bits(z) && finite_bits(e)))
       atomicOr(flags, 4);  // DS_FLAG_NONFINITE
   }
 }
@@ -573,9 +673,13 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
 __global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const double *h, double *hmax) {
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
-  double m = 0.0;
-  for (int j = cell_start[key << xl]; j < cell_start[(key + 1) << xl]; j++) m = fmax(m, h[j]);
-  hmax[key] = m;
+  // maximum as bit patterns (integer pipe): the same value as fmax for h >= 0
+  long long m = 0;
+  for (int j = cell_start[key << xl]; j < cell_start[(key + 1) << xl]; j++) {
+    const long long b = __double_as_longlong(h[j]);
+    m = b > m ? b : m;
+  }
+  hmax[key] = __longlong_as_double(m);
 }
 
 // axis 0: x window, 1: y window, 2: z window (then the radius)
@@ -622,6 +726,16 @@ __global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const
   }
   if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * m);
   else out[key] = m;
+}
+
+// FP32 path origins (TubeDesc::orig), with the same FP64 arithmetic as the
+// per-particle origin it replaces: o + (double)i * w, no contraction.
+__global__ void k_origins(double ox, double wx, int nbx, double oy, double wy, int ny, double oz, double wz, int nz,
+                          double *orig) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nbx) orig[i] = ox + (i * DS_XB) * wx;
+  else if (i < nbx + ny) orig[i] = oy + (i - nbx) * wy;
+  else if (i < nbx + ny + nz) orig[i] = oz + (i - nbx - ny) * wz;
 }
 
 __global__ void k_fill(double *a, int n, double v) {
@@ -708,6 +822,10 @@ void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nse
                            cudaStream_t s) {
   int n = nseg_particles > ncells + 1 ? nseg_particles : ncells + 1;
   k_debug_lists<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, species, st, cell_start, xl, head, next, rawkey);
+}
+void ds_launch_origins(const TubeDesc &T, double *orig, cudaStream_t s) {
+  const int n = T.nbx + T.ny + T.nz;
+  if (n > 0) k_origins<<<blocks_for(n, 256), 256, 0, s>>>(T.ox, T.wx, T.nbx, T.oy, T.wy, T.ny, T.oz, T.wz, T.nz, orig);
 }
 void ds_launch_fill(double *a, int n, double v, cudaStream_t s) {
   if (n > 0) k_fill<<<blocks_for(n, 256), 256, 0, s>>>(a, n, v);

@@ -10,6 +10,8 @@
 #pragma once
 #include <cstdint>
 
+#include "ds_bits.cuh"
+
 #define DS_MAXD 4            // dust species per tube
 #define DS_MAXS (1 + DS_MAXD)  // species per tube (gas + dust)
 
@@ -59,6 +61,14 @@ struct TubeDesc {
   double reach_hmax; // proper grid: largest h whose cut-off 2h the stencil's cells cover
   double rw;         // 1 / (min cell width (1 - 1e-9)): a cut-off c needs ceil(c rw) cells per side
   double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
+  // FP32 path index maps, one FMA and one rounding conversion per axis (GB300's
+  // FP64 pipe runs 2 lanes per SM per clock): fine x index floor(fma(x, kxa,
+  // kxb)) = cell << xl | x bin; cells floor(fma(y, kya, kyb)), floor(fma(z, kza,
+  // kzb)); IDIC cells floor(fma(coordinate, iaa, iab[axis]))
+  double kxa, kxb, kya, kyb, kza, kzb, iaa, iab[3];
+  const double *orig;  // FP32 path: FP64 origins of the nbx x-blocks, the ny y cells, the nz z cells
+  int nbx;
+  int64_t wrap_key[4];  // FP32 path: ds_order_key of oy, ymax, oz, zmax (periodic wrap on the integer pipe)
   // segments
   int seg_begin[DS_MAXS], seg_end[DS_MAXS];
   int key_base[DS_MAXS];   // neighbour keys of species s: key_base[s] + 0..ncells+1
@@ -154,13 +164,17 @@ __device__ __forceinline__ void ds_proper_cell(const TubeDesc &T, double x, doub
   if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
 }
 
-// Proper cell from the reciprocal cell widths (FP32 path: no FP64 divisions;
-// the FP32 path's keys, and so its sorted cells, come from this).
+// FP32 path: fine x index of the keys (the x cell << xl | the x bin within it)
+// and the proper cell, from the index maps (no FP64 division; the FP32 path's
+// keys, and so its sorted cells, come from these).
+__device__ __forceinline__ int ds_fast_fine_x(const TubeDesc &T, double x) {
+  return __double2int_rd(fma(x, T.kxa, T.kxb));
+}
 __device__ __forceinline__ void ds_fast_proper_cell(const TubeDesc &T, double x, double y, double z, int &ix,
                                                     int &iy, int &iz) {
-  ix = (int)floor((x - T.ox) * T.inv_wx);
-  iy = (int)floor((y - T.oy) * T.inv_wy);
-  iz = (int)floor((z - T.oz) * T.inv_wz);
+  ix = ds_fast_fine_x(T, x) >> T.xl;  // arithmetic shift: floor division
+  iy = __double2int_rd(fma(y, T.kya, T.kyb));
+  iz = __double2int_rd(fma(z, T.kza, T.kzb));
   if (T.mode & M_PER_Y) { iy = iy < 0 ? 0 : iy; iy = iy >= T.ny ? T.ny - 1 : iy; }
   if (T.mode & M_PER_Z) { iz = iz < 0 ? 0 : iz; iz = iz >= T.nz ? T.nz - 1 : iz; }
 }

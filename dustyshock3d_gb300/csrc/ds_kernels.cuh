@@ -50,6 +50,7 @@ void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nse
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, int xl, const double *h,
                            double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,
                            const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s);
+void ds_launch_origins(const TubeDesc &T, double *orig, cudaStream_t s);
 void ds_launch_fill(double *a, int n, double v, cudaStream_t s);
 void ds_launch_iota(int *a, int n, cudaStream_t s);
 
