@@ -120,6 +120,10 @@ struct ds_ctx {
   int *inv = nullptr;            // slot of each particle (absolute), all segments
   bool any_bound = false;
   cudaStream_t stream2 = nullptr;
+  // FP32 path with force lists: the overflow walk of the force sweep runs on
+  // its own stream beside the list kernel (they write disjoint particles)
+  cudaStream_t wstream = nullptr;
+  cudaEvent_t e_wfork = nullptr, e_wjoin = nullptr;
   cudaEvent_t e_fork = nullptr, e_up = nullptr, e_dens = nullptr, e_force = nullptr, e_join = nullptr;
   cudaGraphExec_t hgraph[2] = {nullptr, nullptr};
   int side_blocks = 0;  // grid of the transfers overlapped with the step
@@ -404,11 +408,23 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
   }
   if (ev) cudaEventRecord(ev[2], s);
   if (after_density) cudaEventRecord(after_density, s);
+  if (fp32 && c->wstream) {  // the overflow walk beside t_stop, dt and the list kernel
+    cudaEventRecord(c->e_wfork, s);
+    cudaStreamWaitEvent(c->wstream, c->e_wfork, 0);
+    ds_launch_force32_walk(ag, c->any_hpp, depth, c->wstream);
+    cudaEventRecord(c->e_wjoin, c->wstream);
+  }
   DevState st = c->buf[c->parity].view();
   ds_launch_tstop(c->d_tubes, c->d_tstate, c->d_ch_dust, (int)c->ch_dust.size(), st, c->slot_of_pid, c->d_flags, s);
   ds_launch_dt(c->d_tubes, c->d_tstate, c->ntubes, s);
-  if (fp32) ds_launch_force32(ag, c->any_hpp, depth, s);
-  else ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
+  if (fp32 && c->wstream) {
+    ds_launch_force32_list(ag, c->any_hpp, s);
+    cudaStreamWaitEvent(s, c->e_wjoin, 0);
+  } else if (fp32) {
+    ds_launch_force32(ag, c->any_hpp, depth, s);
+  } else {
+    ds_launch_force64(ag, c->any_hpp, c->any_proper, s);
+  }
   if (ev) cudaEventRecord(ev[3], s);
   if (after_force) cudaEventRecord(after_force, s);
   const uint32_t *ik = alt ? c->ikalt : c->ikin;
@@ -646,6 +662,9 @@ ds_status finalize(ds_ctx *c) {
     DA(c->nbl, c->ch_gas.size() * (size_t)c->nbl_cap * DS_CHUNK);
     DA(c->nbl_cnt, N);
     DA(c->nbl_walk, c->ch_gas.size() * (DS_SWEEP_THREADS / 32));
+    CK(cudaStreamCreateWithFlags(&c->wstream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->e_wjoin, cudaEventDisableTiming));
   }
   DA(c->d_cons, 8);
   DA(c->d_flags, 1);
@@ -1659,6 +1678,9 @@ void ds_destroy(ds_ctx *c) {
   for (cudaEvent_t e : evs)
     if (e) cudaEventDestroy(e);
   if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->e_wfork) cudaEventDestroy(c->e_wfork);
+  if (c->e_wjoin) cudaEventDestroy(c->e_wjoin);
+  if (c->wstream) cudaStreamDestroy(c->wstream);
   for (int k = 0; k <= DS_NPHASE; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   for (cudaEvent_t e : c->tev) cudaEventDestroy(e);

@@ -61,3 +61,5 @@ void ds_launch_force64(const SweepArgs &a, bool hpp, bool proper, cudaStream_t s
 void ds_launch_counts64(const SweepArgs &a, bool hpp, bool proper, cudaStream_t s);
 void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cudaStream_t s);
 void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);
+void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s);
+void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);

@@ -343,12 +343,24 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
 
 // With recorded lists: the list kernel, then the walk over overflowed chunks.
 void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) {
+  ds_launch_force32_list(a, hpp, s);
+  ds_launch_force32_walk(a, hpp, depth, s);
+}
+
+// The list kernel alone (no-op without recorded lists).
+void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s) {
+  if (!a.nchunks || !a.nbl) return;
+  const int n = a.nchunks, t = DS_SWEEP_THREADS;
+  if (hpp) k_force32_list<true><<<n, t, 0, s>>>(a);
+  else k_force32_list<false><<<n, t, 0, s>>>(a);
+}
+
+// The walk: every particle without recorded lists, else only the warps the
+// density sweep flagged as overflowed (disjoint from the list kernel's, so the
+// two may run concurrently).
+void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) {
   if (!a.nchunks) return;
   const int n = a.nchunks, t = DS_SWEEP_THREADS;
-  if (a.nbl) {
-    if (hpp) k_force32_list<true><<<n, t, 0, s>>>(a);
-    else k_force32_list<false><<<n, t, 0, s>>>(a);
-  }
   if (depth >= 64) {
     if (hpp) k_force32<true, 64><<<n, t, 0, s>>>(a);
     else k_force32<false, 64><<<n, t, 0, s>>>(a);
