@@ -430,7 +430,7 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
   const uint32_t *ik = alt ? c->ikalt : c->ikin;
   const uint32_t *iv = alt ? c->ivalt : c->ivin;
   ds_launch_idic_reduce(ik, iv, c->N, c->nikeys, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st,
-                        c->ca, s);
+                        c->ca, fp32, s);
   ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, fp32, s);
   ds_launch_relax_move(c->d_tubes, c->d_tstate, c->d_ch_all, (int)c->ch_all.size(), st, c->idic_local, c->edot,
                        c->ca, c->d_flags, fp32, s);

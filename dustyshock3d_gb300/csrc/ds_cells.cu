@@ -232,6 +232,65 @@ __global__ void k_idic_reduce(const uint32_t *islot, int nikeys, const int *seg_
   }
 }
 
+// FP32 path: the same sums with four lanes per key, each over a contiguous
+// quarter of the key's slots in order, the quarters added in order by the
+// key's first lane: four times the threads of the one-lane walk (the FP32
+// path's c2 tube has ~40k keys for 152 SMs, so that walk is latency-bound).
+// The split depends only on the key's own slot count, so a tube sums the same
+// alone and in a batch.
+__global__ void k_idic_reduce4(const uint32_t *islot, int nikeys, const int *seg_key0, const int *seg_species,
+                               const int *seg_orphan, int nseg, DevState st, CellArrays ca) {
+  const unsigned FULL = 0xffffffffu;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int key = (int)(t >> 2), part = (int)(t & 3);
+  bool ok = key < nikeys;
+  int s = 0, r0 = 0, r1 = 0;
+  if (ok) {
+    const int sg = find_seg(seg_key0, nseg, key);
+    ok = key != seg_orphan[sg];  // outside the IDIC grid
+    s = seg_species[sg];
+    r0 = ca.start[key];
+    r1 = ca.start[key + 1];
+  }
+  const int n = r1 - r0;
+  const int a = r0 + (int)(((long long)n * part) >> 2), b = r0 + (int)(((long long)n * (part + 1)) >> 2);
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (ok && s == 0) {
+#pragma unroll 4
+    for (int r = a; r < b; r++) {
+      const int j = (int)islot[r];
+      v[0] = v[0] + st.vx[j];
+      v[1] = v[1] + st.vy[j];
+      v[2] = v[2] + st.vz[j];
+      v[3] = v[3] + st.ax[j];
+      v[4] = v[4] + st.ay[j];
+      v[5] = v[5] + st.az[j];
+    }
+  } else if (ok) {
+#pragma unroll 4
+    for (int r = a; r < b; r++) {
+      const int j = (int)islot[r];
+      v[3] = v[3] + st.ts[j];
+      v[0] = v[0] + st.vx[j];
+      v[1] = v[1] + st.vy[j];
+      v[2] = v[2] + st.vz[j];
+    }
+  }
+  // quarters in order: ((q0 + q1) + q2) + q3 at the key's first lane
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const double q1 = __shfl_down_sync(FULL, v[k], 1), q2 = __shfl_down_sync(FULL, v[k], 2),
+                 q3 = __shfl_down_sync(FULL, v[k], 3);
+    v[k] = ((v[k] + q1) + q2) + q3;
+  }
+  if (!ok || part != 0) return;
+  ca.cnt[key] = n;
+  if (n > 0) {
+    ca.vx[key] = v[0]; ca.vy[key] = v[1]; ca.vz[key] = v[2];
+    ca.a0[key] = v[3]; ca.a1[key] = v[4]; ca.a2[key] = v[5];
+  }
+}
+
 // One component of the per-cell implicit solve (kernel.cu:2310-2437); the
 // reference's two-species operation order when ref2, Sherman-Morrison for any
 // species count otherwise (the same algebra).  ND is a compile-time species
@@ -781,11 +840,15 @@ void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_star
 }
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
-                           cudaStream_t s) {
+                           bool fast, cudaStream_t s) {
   if (nikeys <= 0) return;
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start);
-  k_idic_reduce<<<blocks_for(nikeys, 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st,
-                                                        ca);
+  if (fast)
+    k_idic_reduce4<<<(int)((4LL * nikeys + 127) / 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species,
+                                                                      seg_orphan, nseg, st, ca);
+  else
+    k_idic_reduce<<<blocks_for(nikeys, 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg,
+                                                          st, ca);
 }
 void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
                           int ncell_total, CellArrays ca, bool fast, cudaStream_t s) {

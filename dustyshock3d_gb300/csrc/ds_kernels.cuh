@@ -32,7 +32,7 @@ void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s);
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
-                           cudaStream_t s);
+                           bool fast, cudaStream_t s);
 void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
                           int ncell_total, CellArrays ca, bool fast, cudaStream_t s);
 void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
