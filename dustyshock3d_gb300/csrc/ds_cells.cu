@@ -232,17 +232,19 @@ __global__ void k_idic_reduce(const uint32_t *islot, int nikeys, const int *seg_
   }
 }
 
-// FP32 path: the same sums with four lanes per key, each over a contiguous
-// quarter of the key's slots in order, the quarters added in order by the
-// key's first lane: four times the threads of the one-lane walk (the FP32
-// path's c2 tube has ~40k keys for 152 SMs, so that walk is latency-bound).
+// FP32 path: the same sums with LANES lanes per key, each over a contiguous
+// part of the key's slots in order, the parts added in order by the key's
+// first lane: LANES times the threads of the one-lane walk (the FP32 path's
+// 1.44M-particle tube has ~40k keys for 152 SMs, so that walk is latency-bound).
 // The split depends only on the key's own slot count, so a tube sums the same
 // alone and in a batch.
-__global__ void k_idic_reduce4(const uint32_t *islot, int nikeys, const int *seg_key0, const int *seg_species,
-                               const int *seg_orphan, int nseg, DevState st, CellArrays ca) {
+template <int LANES>
+__global__ void k_idic_reduce_split(const uint32_t *islot, int nikeys, const int *seg_key0, const int *seg_species,
+                                    const int *seg_orphan, int nseg, DevState st, CellArrays ca) {
+  static_assert(LANES == 2 || LANES == 4 || LANES == 8, "lanes per key: a power of two dividing 32");
   const unsigned FULL = 0xffffffffu;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int key = (int)(t >> 2), part = (int)(t & 3);
+  const int key = (int)(t / LANES), part = (int)(t % LANES);
   bool ok = key < nikeys;
   int s = 0, r0 = 0, r1 = 0;
   if (ok) {
@@ -253,7 +255,7 @@ __global__ void k_idic_reduce4(const uint32_t *islot, int nikeys, const int *seg
     r1 = ca.start[key + 1];
   }
   const int n = r1 - r0;
-  const int a = r0 + (int)(((long long)n * part) >> 2), b = r0 + (int)(((long long)n * (part + 1)) >> 2);
+  const int a = r0 + (int)((long long)n * part / LANES), b = r0 + (int)((long long)n * (part + 1) / LANES);
   double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (ok && s == 0) {
 #pragma unroll 4
@@ -276,12 +278,13 @@ __global__ void k_idic_reduce4(const uint32_t *islot, int nikeys, const int *seg
       v[2] = v[2] + st.vz[j];
     }
   }
-  // quarters in order: ((q0 + q1) + q2) + q3 at the key's first lane
+  // the parts in order, (((q0 + q1) + q2) + ...), at the key's first lane
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    const double q1 = __shfl_down_sync(FULL, v[k], 1), q2 = __shfl_down_sync(FULL, v[k], 2),
-                 q3 = __shfl_down_sync(FULL, v[k], 3);
-    v[k] = ((v[k] + q1) + q2) + q3;
+    double sum = v[k];
+#pragma unroll
+    for (int d = 1; d < LANES; d++) sum = sum + __shfl_down_sync(FULL, v[k], d);
+    v[k] = sum;
   }
   if (!ok || part != 0) return;
   ca.cnt[key] = n;
@@ -838,14 +841,17 @@ void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s) {
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start);
 }
+#ifndef DS_IDIC_LANES
+#define DS_IDIC_LANES 4  // lanes per IDIC key of the FP32 path's cell sums (measured: 4 beats 8)
+#endif
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
                            bool fast, cudaStream_t s) {
   if (nikeys <= 0) return;
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start);
   if (fast)
-    k_idic_reduce4<<<(int)((4LL * nikeys + 127) / 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species,
-                                                                      seg_orphan, nseg, st, ca);
+    k_idic_reduce_split<DS_IDIC_LANES><<<(int)(((long long)DS_IDIC_LANES * nikeys + 127) / 128), 128, 0, s>>>(
+        islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca);
   else
     k_idic_reduce<<<blocks_for(nikeys, 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg,
                                                           st, ca);
