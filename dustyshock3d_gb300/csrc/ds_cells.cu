@@ -13,8 +13,10 @@
 //                  copies; IDIC key per slot, scattered to caller-index order
 //   k_cell_start   first sorted slot of every key
 //   (radix sort)   IDIC keys, stable
-//   (sweeps)       density + EOS (+ dust density), t_stop, dt, force
+//   (sweeps)       density + EOS (+ dust density), t_stop, dt, force (FP32 path:
+//                  the force walk of overflowed warps on a second stream)
 //   k_idic_reduce  per IDIC cell and species: count, sum v, sum t_stop / sum A
+//                  (FP32 path: k_idic_reduce_split, several lanes per cell)
 //   k_idic_solve   per IDIC cell: means, eps, the implicit drag solve
 //   k_relax_move   per particle: relax to the cell solution, move, energy
 //   k_step_end     per tube: Tm += dt
