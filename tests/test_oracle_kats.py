@@ -55,6 +55,34 @@ def test_idic_two_species_reference_order_equals_sherman_morrison():
         assert np.allclose(d1, d2, rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_idic_solve_equals_the_implicit_system(n):
+    """The per-cell solve is the implicit drag step of every species at once:
+    v_g' = v_g + tau Psi - tau sum_k eps_k (v_g' - v_k') / t_k and
+    v_k' = v_k + tau (v_g' - v_k') / t_k, solved here directly as an
+    (N+1) x (N+1) linear system for random cells."""
+    rng = np.random.default_rng(100 + n)
+    for _ in range(200):
+        eps = rng.uniform(0.01, 5, n)
+        t = 10 ** rng.uniform(-4, 0, n)
+        vg, psi, tau = rng.normal(), rng.normal(), 10 ** rng.uniform(-4, -2)
+        vd = rng.normal(size=n)
+        A = np.zeros((n + 1, n + 1))
+        b = np.zeros(n + 1)
+        A[0, 0] = 1 + tau * np.sum(eps / t)
+        A[0, 1:] = -tau * eps / t
+        b[0] = vg + tau * psi
+        for k in range(n):
+            A[k + 1, 0] = -tau / t[k]
+            A[k + 1, k + 1] = 1 + tau / t[k]
+            b[k + 1] = vd[k]
+        x = np.linalg.solve(A, b)
+        g, d = orc.solve_cell(eps, t, vg, vd, psi, tau)
+        scale = np.abs(x).max()
+        assert abs(g - x[0]) <= 1e-12 * scale
+        assert np.abs(np.asarray(d) - x[1:]).max() <= 1e-12 * scale
+
+
 def test_idic_conserves_cell_momentum():
     """Without Psi the drag only exchanges momentum: v_g + sum eps_k v_k is kept."""
     eps, t = [0.7, 2.0, 0.1], [1e-3, 3e-2, 1e-4]
