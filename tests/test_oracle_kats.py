@@ -126,3 +126,28 @@ def test_split_species_moves_the_gas_as_one():
         assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), f
     for k in (1, 2, 3):
         assert np.abs(B.species[k].vx - A.species[1].vx).max() <= 1e-12 * np.abs(A.species[1].vx).max(), k
+
+
+def test_cfl_step_is_the_smallest_signal_crossing_time():
+    """CFL step (extension; the reference steps by a fixed tau): tau = cfl x
+    min over free gas particles of h_i / (c_i + |v_i|), with c from the step's
+    own density and pressure and v from the step's start, clamped to T_end."""
+    from dustyshock3d_gb300 import ic
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, x_range=(-0.25, 0.25))
+    assert P.mode.cfl
+    g0 = sp[0].copy().fill_missing()
+    rng = np.random.default_rng(5)
+    g0.vx = rng.normal(scale=0.3, size=g0.n)  # velocities that matter against c
+    species = [g0, sp[1].copy().fill_missing()]
+    O = orc.OracleState(P, species).step(1)
+    g1 = O.species[0]
+    free = g0.ind == 0
+    c = np.sqrt(P.Gam_g * g1.p[free] / g1.rho[free])
+    v = np.sqrt(g0.vx[free] ** 2 + g0.vy[free] ** 2 + g0.vz[free] ** 2)
+    want = P.cfl * np.min(g0.h[free] / (c + v))
+    assert O.last_dt == pytest.approx(want, rel=1e-14)
+    assert O.Tm == O.last_dt
+    P2 = P.copy()
+    P2.T_end = 0.5 * want  # the first step stops at T_end
+    O2 = orc.OracleState(P2, species).step(1)
+    assert O2.last_dt == P2.T_end and O2.Tm == P2.T_end
