@@ -458,7 +458,7 @@ __device__ __forceinline__ void idic_solve_cell_fast(const TubeDesc &T, int c, d
 // of each species: new velocities; for gas Psi; for dust the mean t_stop and eps.
 template <int ND, bool FAST>
 __device__ __forceinline__ void idic_solve_cell(const TubeDesc &T, int c, double tau, CellArrays &ca) {
-  if (FAST) {
+  if constexpr (FAST) {
     idic_solve_cell_fast<ND>(T, c, tau, ca);
     return;
   }
