@@ -18,6 +18,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // driver types only (CUcontext, CUresult); libcuda is not linked
 #include <cuda_runtime.h>
 
 #include "../../include/dustyshock3d_gb300.h"
@@ -1468,6 +1469,33 @@ ds_status ds_save_tube(ds_ctx *c, int tube, const char *path) {
   return DS_OK;
 }
 
+}  // extern "C"
+
+// The first run parameter that differs between a checkpoint's parameters and
+// the tube's, by name, or nullptr.  Compared: everything that changes the
+// physics, the grids or the step (box, equation of state, h, cell widths,
+// fixed step, AV constants, gamma, sound speed, species and their constants,
+// mode bits, precision, stencil, CFL number, empty-cell defaults).  Not
+// compared: T_end and T_out (a resumed run may go further), Maximum_particle
+// and Particle_on_length (initial conditions only), list_depth and force_list
+// (tuning choices that leave the results unchanged).
+static const char *checkpoint_param_mismatch(const ds_params &a, const ds_params &b) {
+#define DS_CK_FIELD(f) \
+  if (!(a.f == b.f)) return #f;
+  DS_CK_FIELD(X_min) DS_CK_FIELD(X_max) DS_CK_FIELD(Y_min) DS_CK_FIELD(Y_max) DS_CK_FIELD(Z_min)
+  DS_CK_FIELD(Z_max) DS_CK_FIELD(Type_of_state) DS_CK_FIELD(h) DS_CK_FIELD(Coeff_h_dust_cell) DS_CK_FIELD(tau)
+  DS_CK_FIELD(alpha) DS_CK_FIELD(beta) DS_CK_FIELD(eps) DS_CK_FIELD(Gam_g) DS_CK_FIELD(Speed_of_sound_gas)
+  DS_CK_FIELD(n_dust) DS_CK_FIELD(mode) DS_CK_FIELD(precision) DS_CK_FIELD(stencil) DS_CK_FIELD(cell_w)
+  DS_CK_FIELD(idic_w) DS_CK_FIELD(cfl) DS_CK_FIELD(t_empty)
+  for (int k = 0; k < DS_MAX_DUST && k < a.n_dust; k++) {
+    DS_CK_FIELD(mass_ratio[k]) DS_CK_FIELD(R_dust[k]) DS_CK_FIELD(t_stop_const[k]) DS_CK_FIELD(eps_empty[k])
+  }
+#undef DS_CK_FIELD
+  return nullptr;
+}
+
+extern "C" {
+
 ds_status ds_load_tube(ds_ctx *c, int tube, const char *path) {
   if (!c || !path) return DS_ERR_ARG;
   if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
@@ -1483,17 +1511,29 @@ ds_status ds_load_tube(ds_ctx *c, int tube, const char *path) {
       fread(&nsp, sizeof nsp, 1, F.f) != 1)
     return fail(c, DS_ERR_IO, std::string("not a checkpoint: ") + path);
   if (nsp != 1 + c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "checkpoint species count differs from the tube's");
+  const char *differs = checkpoint_param_mismatch(P, c->params[tube]);
+  if (differs)
+    return fail(c, DS_ERR_ARG, std::string("checkpoint was saved with a different ") + differs + " than the tube's");
+  // Every species is read and checked before any is written, so a bad file
+  // leaves the tube as it was.
+  std::vector<long long> counts(nsp);
+  std::vector<std::vector<double>> bufs(nsp);
+  std::vector<std::vector<int>> inds(nsp);
   for (int s = 0; s < nsp; s++) {
     long long n = 0;
     if (fread(&n, sizeof n, 1, F.f) != 1 || n < 0 || n > INT32_MAX) return fail(c, DS_ERR_IO, "truncated checkpoint");
-    std::vector<double> buf((size_t)NF * (size_t)(n > 0 ? n : 1));
-    std::vector<int> ind((size_t)(n > 0 ? n : 1));
-    if (n > 0 && (fread(buf.data(), sizeof(double), (size_t)NF * n, F.f) != (size_t)NF * n ||
-                  fread(ind.data(), sizeof(int), (size_t)n, F.f) != (size_t)n))
+    counts[s] = n;
+    bufs[s].resize((size_t)NF * (size_t)(n > 0 ? n : 1));
+    inds[s].resize((size_t)(n > 0 ? n : 1));
+    if (n > 0 && (fread(bufs[s].data(), sizeof(double), (size_t)NF * n, F.f) != (size_t)NF * n ||
+                  fread(inds[s].data(), sizeof(int), (size_t)n, F.f) != (size_t)n))
       return fail(c, DS_ERR_IO, "truncated checkpoint");
+  }
+  for (int s = 0; s < nsp; s++) {
+    const long long n = counts[s];
     const double *f[NF];
-    for (int k = 0; k < NF; k++) f[k] = buf.data() + (size_t)k * (size_t)n;
-    ds_status st = set_species(c, tube, s, (int)n, f, ind.data());
+    for (int k = 0; k < NF; k++) f[k] = bufs[s].data() + (size_t)k * (size_t)n;
+    ds_status st = set_species(c, tube, s, (int)n, f, inds[s].data());
     if (st != DS_OK) return st;
   }
   if (c->finalized) {  // resident context: set the clock now
@@ -1705,6 +1745,13 @@ void ds_destroy(ds_ctx *c) {
 // (different streams, or different host threads) race on it.  Every scratch
 // word a call reads has been written earlier in the same call, so nothing
 // needs clearing between calls.
+//
+// The array belongs to this library's device code, which the CUDA runtime
+// loads into a device's context only when first used there (lazy module
+// loading is the default).  That load takes device memory through the driver,
+// and the first call on each device is what triggers it, together with the
+// address set-up below.  A host that hands the rest of the memory to its pool
+// makes that first call before it does so, and before any stream capture.
 // ===========================================================================
 namespace {
 
@@ -1716,21 +1763,67 @@ constexpr size_t kNaWords = 4 * (size_t)kNaMax + kNaHistWords;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
 
 std::mutex g_noalloc_mu;
-uint32_t *g_noalloc_ptr[256] = {};
+
+// The scratch array's device address, per device, with the ID of the context
+// it was resolved in.  Context IDs are unique for the life of the process, so
+// a context re-created after cudaDeviceReset does not match a stale entry.
+struct NoallocSlot {
+  unsigned long long ctx_id;
+  uint32_t *ptr;
+};
+NoallocSlot g_noalloc_slot[256] = {};
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+
+// ID of the context current on this thread, 0 if none is current or the driver
+// does not offer the query.  The two driver functions are fetched through the
+// runtime, so the library does not link libcuda itself.  Caller holds
+// g_noalloc_mu.
+unsigned long long current_ctx_id() {
+  static bool looked_up = false;
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!looked_up) {
+    looked_up = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+  }
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // The device address of the scratch array for the current device.  The host
-// symbol is only a stand-in: it is resolved with cudaGetSymbolAddress once per
-// device (on the first call made with that device current).
+// symbol is only a stand-in: the set-up resolves it with cudaGetSymbolAddress
+// on the first call made with the device current, and again whenever the
+// device's context has changed since (a cudaDeviceReset in between).  Where the
+// context cannot be identified, it is resolved on every call.
 ds_status noalloc_scratch(uint32_t **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return DS_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return DS_ERR_CUDA;
-    g_noalloc_ptr[dev] = (uint32_t *)p;
+  NoallocSlot &slot = g_noalloc_slot[dev];
+  const unsigned long long id = current_ctx_id();
+  if (slot.ptr && id != 0 && slot.ctx_id == id) {
+    *out = slot.ptr;
+    return DS_OK;
   }
-  *out = g_noalloc_ptr[dev];
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return DS_ERR_CUDA;
+  slot.ptr = (uint32_t *)p;
+  slot.ctx_id = current_ctx_id();  // the context is current now
+  *out = slot.ptr;
   return DS_OK;
 }
 
@@ -1789,12 +1882,21 @@ extern "C" ds_status ds_cell_lists_noalloc(const ds_params *p, int n, const doub
   uint32_t *hist = s + 4 * (size_t)kNaMax;
   cudaStream_t cs = (cudaStream_t)stream;
   const int nh = T.ncells + 1;
-  k_na_fill<<<(nh + 255) / 256, 256, 0, cs>>>(d_head, nh, -1);
+  // Each launch's own status is checked; the thread's last-error state is not
+  // read, so an earlier failure of someone else's call is not reported here.
+  cudaError_t e = ds_launch(k_na_fill, dim3((nh + 255) / 256), dim3(256), cs, d_head, nh, -1);
   if (n > 0) {
-    k_na_keys<<<(n + 255) / 256, 256, 0, cs>>>(T, d_x, d_y, d_z, n, d_cell_key, kin, vin);
     bool alt = false;
-    ds_radix_sort(kin, vin, kalt, valt, n, bits_for((long long)T.ncells + 2), hist, cs, &alt);
-    k_na_lists<<<(n + 255) / 256, 256, 0, cs>>>(alt ? kalt : kin, alt ? valt : vin, n, T.ncells, d_head, d_next);
+    if (e == cudaSuccess)
+      e = ds_launch(k_na_keys, dim3((n + 255) / 256), dim3(256), cs, T, d_x, d_y, d_z, n, d_cell_key, kin, vin);
+    if (e == cudaSuccess) e = ds_radix_sort(kin, vin, kalt, valt, n, bits_for((long long)T.ncells + 2), hist, cs, &alt);
+    if (e == cudaSuccess)
+      e = ds_launch(k_na_lists, dim3((n + 255) / 256), dim3(256), cs, (const uint32_t *)(alt ? kalt : kin),
+                    (const uint32_t *)(alt ? valt : vin), n, T.ncells, d_head, d_next);
   }
-  return cudaGetLastError() == cudaSuccess ? DS_OK : DS_ERR_CUDA;
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // the failed launch recorded e there; it is reported by the status
+    return DS_ERR_CUDA;
+  }
+  return DS_OK;
 }

@@ -189,12 +189,16 @@ cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, ui
     const int shift = p * width;
     int bits = key_bits - shift < width ? key_bits - shift : width;
     const uint32_t mask = (1u << bits) - 1u;
-    rs_hist<<<ntiles, RS_THREADS, 0, stream>>>(ki, n, shift, mask, hist, ntiles);
-    rs_rowscan<<<(int)mask + 1, 256, 0, stream>>>(hist, ntiles, totals);
-    rs_scatter<<<ntiles, RS_THREADS, 0, stream>>>(ki, vi, ko, vo, n, shift, mask, hist, ntiles, totals);
+    cudaError_t e = ds_launch(rs_hist, dim3(ntiles), dim3(RS_THREADS), stream, ki, n, shift, mask, hist, ntiles);
+    if (e == cudaSuccess)
+      e = ds_launch(rs_rowscan, dim3((int)mask + 1), dim3(256), stream, hist, ntiles, totals);
+    if (e == cudaSuccess)
+      e = ds_launch(rs_scatter, dim3(ntiles), dim3(RS_THREADS), stream, ki, vi, ko, vo, n, shift, mask, hist,
+                    ntiles, totals);
+    if (e != cudaSuccess) return e;
     uint32_t *t = ki; ki = ko; ko = t;
     t = vi; vi = vo; vo = t;
   }
   *result_in_alt = (passes & 1) != 0;
-  return cudaGetLastError();
+  return cudaSuccess;
 }

@@ -3,6 +3,21 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <utility>
+
+// Launches kernel k and returns the status of that launch alone (the value
+// cudaLaunchKernelEx returns), without reading or clearing the thread's
+// last-error state, so an earlier unrelated error is neither consumed nor
+// blamed on this launch.
+template <class... KArgs, class... Args>
+static inline cudaError_t ds_launch(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Keys per radix tile and the most digit values of one pass (histogram rows).
 constexpr int DS_RADIX_TILE = 2048;
@@ -14,6 +29,8 @@ int ds_radix_passes(int key_bits);
 
 // Sorts the low key_bits of keys[0..n) with their vals, stably.  The sorted
 // pairs end in (keys, vals) or, when *result_in_alt, in (keys_alt, vals_alt).
-// Launch-only: capturable into a CUDA graph.
+// Launch-only: capturable into a CUDA graph.  Returns the first failed
+// launch's status (cudaSuccess if every pass launched); the thread's
+// last-error state is left as the launches left it.
 cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, int n,
                           int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt);

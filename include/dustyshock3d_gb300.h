@@ -396,10 +396,15 @@ ds_status ds_last_error(ds_ctx *c, int *device_flags, char *msg, int msglen);
  * d_next[n], d_head[head_len] with head_len >= Number_of_fihd_cells + 1.
  * The grid comes from p (cell width, box, DS_MODE_GRID_PROPER/PERIODIC_*).
  * Work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
- * and the call returns without waiting.  The first call on each device
- * resolves the scratch array's device address; make that first call before
- * any stream capture.  All calls share the one scratch array, so calls whose
- * work overlaps on the GPU race; serialise them. */
+ * and the call returns without waiting.  The first call on each device (and
+ * the first after a cudaDeviceReset) loads the library's device code and its
+ * static array into that device's context and resolves the array's device
+ * address: the load itself takes device memory through the driver, so make
+ * that first call before the host's pool takes the memory, and before any
+ * stream capture.  Each launch's status is checked on its own; an earlier
+ * error of another call on the thread is neither cleared nor reported.  All
+ * calls share the one scratch array, so calls whose work overlaps on the GPU
+ * race; serialise them. */
 #define DS_NOALLOC_MAX_PARTICLES 262144
 ds_status ds_cell_lists_noalloc(const ds_params *p, int n, const double *d_x, const double *d_y,
                                 const double *d_z, int *d_cell_key, int *d_head, int head_len, int *d_next,

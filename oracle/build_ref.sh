@@ -8,10 +8,15 @@
 #   the "\Nn" escape in one snapshot header string (kernel.cu:455; MSVC reads an
 #   unknown escape as the bare letter, g++ refuses it)  ->  "Nn"
 # everything else compiles as written against oracle/ref_include/cuda_runtime.h.
-# Needs the reference tree (default /root/reference); exits 3 when it is absent.
+# Needs the reference tree, named by DS_REFERENCE_DIR (there is no default);
+# exits 3 when the variable is unset or the sources are not there.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${DS_REFERENCE_DIR:-/root/reference}"
+if [ -z "${DS_REFERENCE_DIR:-}" ]; then
+  echo "DS_REFERENCE_DIR is not set: point it at the reference tree (kernel.cu, IDIC.h, data.h)" >&2
+  exit 3
+fi
+REF="$DS_REFERENCE_DIR"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/kernel.cu" ] || [ ! -f "$REF/IDIC.h" ] || [ ! -f "$REF/data.h" ]; then
   echo "reference sources not found under $REF" >&2

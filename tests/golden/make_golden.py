@@ -7,8 +7,8 @@ averaging and solve) on small Init.txt files, and stores what its snapshot
 writers print (``Data_out`` / ``Data_out_dust``, kernel.cu:232-826, printed
 with ``%10.8lf``) as compressed .npz fixtures next to this script.
 
-Needs the reference tree (default /root/reference, or DS_REFERENCE_DIR); run it
-in a checkout that has one:  python tests/golden/make_golden.py
+Needs the reference tree, named by the DS_REFERENCE_DIR environment variable
+(there is no default); run it in a checkout that has one:  python tests/golden/make_golden.py
 The fixtures are small and committed; tests only read them.
 """
 from __future__ import annotations
@@ -71,6 +71,8 @@ def _read(path):
 
 
 def build_reference() -> str:
+    if not os.environ.get("DS_REFERENCE_DIR"):
+        raise SystemExit("DS_REFERENCE_DIR is not set: point it at the reference tree (kernel.cu, IDIC.h, data.h)")
     r = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True, capture_output=True, text=True)
     return r.stdout.strip().splitlines()[-1]
 

@@ -267,6 +267,28 @@ def test_checkpoint_resume(precision, tmp_path):
                 assert np.abs(a - b).sum() / np.abs(b).sum() < 1e-6, (s, f)
 
 
+def test_checkpoint_with_other_run_parameters_is_refused(tmp_path):
+    """A checkpoint saved under other physics (here another stopping time, then
+    another h layout) is DS_ERR_ARG, and the tube keeps its own state."""
+    P, sp = small_tube()
+    path = str(tmp_path / "tube.ckpt")
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(2)
+        S.save(0, path)
+    for other in (small_tube(t_s=1e-2), small_tube(h_factor=1.2)):
+        P2, sp2 = other
+        with Solver(P2) as S:
+            S.set_tube(0, sp2)
+            S.step(1)
+            before = [S.get_species(0, s) for s in range(2)]
+            assert S.L.ds_load_tube(S.ctx, 0, path.encode()) == 1
+            after = [S.get_species(0, s) for s in range(2)]
+            for s in range(2):
+                for f in ("x", "vx", "rho"):
+                    assert_equal_nan(getattr(after[s], f), getattr(before[s], f), f"species {s} {f}")
+
+
 def test_batched_tubes_equal_single_runs():
     cases = [small_tube(eps=1.0, t_s=1e-3), small_tube(eps=0.1, t_s=1e-2, rho_R=0.25, p_R=0.2),
              small_tube(dx_left=1 / 48, Ly=0.375, eps=3.0, t_s=3e-4)]
