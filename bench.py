@@ -63,11 +63,15 @@ def parse():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--rate", type=float, default=4.0, help="serve: mean arrivals per second")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
+    ap.add_argument("--compare", type=int, default=16,
+                    help="serve: requests (first by arrival) also served alone and solved one at a time")
     ap.add_argument("--host-ic", action="store_true",
                     help="serve: make initial particles on the host and upload them (default: on the device)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="default line: skip the 11.5M-particle tube record")
+    ap.add_argument("--no-batch", action="store_true", help="default line: skip the 64-tube batch record")
     ap.add_argument("--t-end", type=float, default=0.2, help="accuracy_720k: end time of every run")
     return ap.parse_args()
 
@@ -202,11 +206,95 @@ def time_cpu(name, steps, budget_s=25.0):
     return n * done / el, f"{done} FP64 step(s) of the full {n}-particle tube from t=0 ({el:.1f} s)", n
 
 
+def batch64_tubes(seed):
+    """The 64 seeded uneven tubes (ic.batch_tubes' draws), as device generators:
+    (params, DeviceIC) pairs, so that no particle is made on the host."""
+    import numpy as np
+
+    from dustyshock3d_gb300 import ic
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(64):
+        spec = ic.DeviceIC.uneven(**ic.draw_tube_params(rng))
+        out.append((spec.plan()[0], spec))
+    return out
+
+
+def batch64_record(seed, steps, warmup, shard=None):
+    """Batched FP32: the 64 uneven tubes in one context, cell size and list
+    depth chosen by the autotuner on the first 8; CUDA events around exactly
+    `steps` replays of the step graphs.  Returns (record, n_particles_all)."""
+    from dustyshock3d_gb300 import tune
+    from dustyshock3d_gb300.solver import Solver
+    all_tubes = batch64_tubes(seed)
+    sizes = [sum(spec.plan()[1]) for _, spec in all_tubes]
+    idx = list(range(64)) if shard is None else shard
+    tubes = [all_tubes[i] for i in idx]
+    t0 = time.perf_counter()
+    choice, log = tune.tune(tubes, sample=8)
+    tune_s = time.perf_counter() - t0
+    ps = []
+    for P, _ in tubes:
+        Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth)
+        Q.precision = "fp32"
+        ps.append(Q)
+    n = sum(sizes[i] for i in idx)
+    with Solver(ps) as S:
+        for t, (_, spec) in enumerate(tubes):
+            S.init_tube(t, spec)
+        S.step(warmup)
+        total_ms = S.step_timed_graph(steps)  # the graphs ds_step replays
+        _, phase = S.step_timed(steps)         # phase split, after the timed region
+        kps = S.kernels_per_step()
+        mem = S.memory_bytes()
+    rec = {"value": n * steps / (total_ms * 1e-3), "ms_per_step": total_ms / steps, "steps": steps,
+           "warmup": warmup, "tubes": len(tubes), "particles": n, "seed": seed,
+           "initial_conditions": "generated on the device (ds_init_tube)",
+           "autotuned": dataclasses.asdict(choice), "tuning_s": tune_s,
+           "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, ms=d) for a, b, c, d in log],
+           "device_bytes": mem,
+           "phase_ms_per_step": {k: v / steps for k, v in zip(("sort", "density", "force", "idic_update"), phase)},
+           "gpu_launches": kps * steps}
+    return rec, sum(sizes), total_ms
+
+
+def device_tube_record(name, steps32=10, steps64=2, warmup=2):
+    """One tube generated on the device, timed on the FP32 and the FP64 path
+    (CUDA events around the step graphs, after warm-up steps)."""
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300.solver import Solver
+    dx, Ly, desc = WORKLOADS[name]
+    spec = ic.DeviceIC.dusty_sod(dx_left=dx, Ly=Ly)
+    P, counts = spec.plan()
+    n = sum(counts)
+    out = {"workload": name, "description": desc, "particles": n, "gas": counts[0]}
+    for prec, steps, wu in (("fp32", steps32, warmup), ("fp64", steps64, 1)):
+        Q = P.copy()
+        Q.precision = prec
+        with Solver(Q) as S:
+            S.init_tube(0, spec)
+            S.step(wu)
+            ms = S.step_timed_graph(steps)
+            rec = {"value": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps, "warmup": wu}
+            if prec == "fp32":
+                _, phase = S.step_timed(steps)
+                rec["phase_ms_per_step"] = {k: v / steps for k, v in
+                                            zip(("sort", "density", "force", "idic_update"), phase)}
+        out[prec] = rec
+    return out
+
+
 def cores():
     try:
         return len(os.sched_getaffinity(0))
     except AttributeError:
         return os.cpu_count() or 1
+
+
+def workload_config(name, n, n_gas, ws):
+    """The `config` of a line: what the workload is, the same for both arms."""
+    return {"workload": name, "description": WORKLOADS[name][2], "particles": n, "gas": n_gas,
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single tube"}
 
 
 def run_reference(args):
@@ -242,7 +330,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": name, "description": WORKLOADS[name][2], "particles": n},
+            "config": workload_config(name, n, sp[0].n, 1),
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -281,6 +369,47 @@ def density_bytes_per_particle(hpp: bool) -> int:
     per-particle h), rho, p, e (24), vx, vy, vz (24, CFL bound), Ind and the
     own cell key (8); write rho, p (16), hyd32 (16), the list count (4)."""
     return 32 + (8 if hpp else 0) + 24 + 24 + 8 + 16 + 16 + 4
+
+
+def profile_value(path, key):
+    """A `key: value` line of a committed ncu summary, or None."""
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def sm_count():
+    try:
+        import torch
+        return int(torch.cuda.get_device_properties(0).multi_processor_count)
+    except Exception:  # noqa: BLE001 - reported as unknown
+        return None
+
+
+def issue_ceiling(profile, n_gas, launch_ms, clk):
+    """The ceiling that binds the density sweep: warp-instruction issue.  Each
+    SM issues at most 4 warp instructions per clock (one per sub-partition), so
+    a launch of I warp instructions needs I / (4 SMs f) seconds at SM clock f.
+    I per launch: the committed ncu capture's count per gas particle times the
+    gas particles; f: the median SM clock sampled during this run."""
+    per = profile_value(profile, "warp_instructions_per_particle")
+    sms = sm_count()
+    if per is None or sms is None or not clk or not clk.get("sm_mhz"):
+        return None
+    inst = per * n_gas
+    slots = 4 * sms * clk["sm_mhz"] * 1e6 * launch_ms * 1e-3
+    return {"bound": "issue", "warp_instructions_per_launch": inst, "issue_slots_per_launch": slots,
+            "frac": inst / slots, "sms": sms, "sm_mhz": clk["sm_mhz"],
+            "note": "warp instructions / (4 x SMs x SM clock x launch time); instructions from the ncu capture"}
+
+
+def batch64_sizes(seed):
+    return [sum(spec.plan()[1]) for _, spec in batch64_tubes(seed)]
 
 
 def force_bytes_per_particle(fp32: bool, hpp: bool) -> int:
@@ -393,7 +522,13 @@ def run_ours(args):
     # one with events between phases), then the recorded force neighbours of
     # the final state (0 < r < 2 max(h_i, h_j), counted by the parity hook)
     _, phase = S.step_timed(args.steps)
-    list_entries = int(S.debug_cells(0, 0)["nnb"][S.get_species(0, 0).ind == 0].sum())
+    dbg = S.debug_cells(0, 0)
+    free = S.get_species(0, 0).ind == 0
+    list_entries = int(dbg["nnb"][free].sum())
+    cand_per_pair = {"stencil_cells": float(dbg["ncand"][free].sum() / max(list_entries, 1)),
+                     "note": "particles in the cells of each gas particle's stencil per recorded pair "
+                             "(0 < r < 2 max(h_i, h_j)); the FP32 walk screens only the x window of each row, "
+                             "about 2/3 of these"}
     S.close()
 
     fp64 = None
@@ -417,6 +552,13 @@ def run_ours(args):
         fp64["l1_fp32_vs_fp64"] = {"rho_gas": rel(g32.rho, g64.rho), "v_gas": rel(g32.vx, g64.vx),
                                    "v_dust": rel(d32.vx, d64.vx), "t_fp32": t32[0], "t_fp64": t64[0],
                                    "steps": args.warmup + args.steps}
+        if not args.no_e2e:  # the same-precision end-to-end number
+            barrier(dist)
+            el, h2d, d2h = e2e_run(P, sp, args.steps, 1, bound=True)
+            el = dist_max(dist, el)
+            fp64["e2e"] = {"value": ws * n * args.steps / el, "unit": "particle-steps/s",
+                           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / args.steps,
+                           "path": "as the headline e2e (ds_bind_host + ds_step_host(1) per step), fp64 path"}
 
     e2e = None
     if not args.no_e2e:
@@ -433,6 +575,18 @@ def run_ours(args):
         e2e["separate_calls"] = {"value": ws * n * args.steps / el2, "h2d_bytes_per_step": h2d2,
                                  "d2h_bytes_per_step": d2h2, "ms_per_step": 1e3 * el2 / args.steps,
                                  "path": "ds_upload_gas/dust (pinned) + ds_step(1) + ds_download_gas/dust"}
+    c3 = None
+    if not args.no_c3 and name == DEFAULT_WORKLOAD:
+        barrier(dist)
+        c3 = device_tube_record("dusty_sod_5760k")
+    batch = None
+    if not args.no_batch and name == DEFAULT_WORKLOAD:
+        barrier(dist)
+        shard = balanced_shards(batch64_sizes(args.seed), ws)[rank] if ws > 1 else None
+        batch, n_batch_all, bms = batch64_record(args.seed, 10, 3, shard)
+        bms = dist_max(dist, bms)
+        batch["value"] = n_batch_all * 10 / (bms * 1e-3)  # whole job: all 64 tubes over the slowest rank
+        batch["ms_per_step"] = bms / 10
     clk = clocks.stop()
 
     if rank != 0:
@@ -449,6 +603,9 @@ def run_ours(args):
             "list_entries_per_launch": list_entries,
             "note": "issue-bound, not HBM-bound: every particle screens the candidates of 27 (or 125) cells "
                     "in FP32; traffic from the committed ncu capture of this workload"}
+    roof["issue"] = issue_ceiling(os.path.join(ROOT, "profiles", "density32_dusty_sod_720k.txt"), n_gas, dens_ms,
+                                  clk)
+    roof["candidates_per_pair"] = cand_per_pair
     cpu = None
     if not args.no_cpu_baseline:
         v, sample, _ = time_cpu(name, 3)
@@ -457,112 +614,106 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": name, "description": WORKLOADS[name][2], "particles": n, "gas": n_gas,
-                       "precision": "fp32 neighbour sums (Kahan), fp64 state / IDIC / sums",
-                       "l2": "inputs larger than L2 (resident state ~%d MB)" % (n * 256 // 2 ** 20),
-                       "timing": "CUDA events around the step graphs ds_step replays, on the context's stream; "
-                                 "phase split from a second pass with events between phases",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single tube"},
+            "config": workload_config(name, n, n_gas, ws),
+            "precision": "fp32 neighbour sums (Kahan), fp64 state / IDIC / sums",
+            "l2": "inputs larger than L2 (resident state ~%d MB)" % (n * 256 // 2 ** 20),
+            "timing": "CUDA events around the step graphs ds_step replays, on the context's stream; "
+                      "phase split from a second pass with events between phases",
             "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
                                                                      phase)},
             "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "dusty_sod_5760k": c3, "batch64": batch,
             "gpu_launches": kps * args.steps, "clocks": clk}
     print(json.dumps(line))
     return 0
 
 
 def run_batch(args):
-    """64 uneven tubes (seeded) advanced together, FP32, autotuned.  With N
-    ranks the tubes are split over the GPUs (balanced by particle count; the
-    tubes are independent, so no collective touches the data path)."""
-    from dustyshock3d_gb300 import ic, tune
-    from dustyshock3d_gb300.solver import Solver
+    """64 uneven tubes (seeded) advanced together, FP32, autotuned, generated on
+    the device.  With N ranks the tubes are split over the GPUs (balanced by
+    particle count; the tubes are independent, so no collective touches the data
+    path)."""
     ws, rank, dist = dist_setup()
-    all_tubes = ic.batch_tubes(seed=args.seed, n_tubes=64)
-    shards = balanced_shards([sum(s.n for s in sp) for _, sp in all_tubes], ws)
-    tubes = [all_tubes[i] for i in shards[rank]]
-    n_all = sum(sum(s.n for s in sp) for _, sp in all_tubes)
-    choice, log = tune.tune(tubes, sample=8)
-    ps = []
-    for P, _ in tubes:
-        Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth)
-        Q.precision = "fp32"
-        ps.append(Q)
-    n = sum(sum(s.n for s in sp) for _, sp in tubes)
+    shard = balanced_shards(batch64_sizes(args.seed), ws)[rank] if ws > 1 else None
     clocks = ClockSampler(0)
     clocks.start()
-    with Solver(ps) as S:
-        for t, (_, sp) in enumerate(tubes):
-            S.set_tube(t, sp)
-        S.step(args.warmup)
-        barrier(dist)
-        total_ms = S.step_timed_graph(args.steps)  # the graphs ds_step replays
-        _, phase = S.step_timed(args.steps)         # phase split, after the timed region
-        kps = S.kernels_per_step()
-        mem = S.memory_bytes()
+    rec, n_all, total_ms = batch64_record(args.seed, args.steps, args.warmup, shard)
     clk = clocks.stop()
     total_ms = dist_max(dist, total_ms)
     if rank != 0:
         return 0
     value = n_all * args.steps / (total_ms * 1e-3)
+    cfg = {"workload": "batch64", "tubes": 64, "particles": n_all, "seed": args.seed,
+           "tubes_on_rank0": rec["tubes"], "particles_on_rank0": rec["particles"]}
+    for k in ("autotuned", "tuning_s", "tuning_log", "device_bytes", "initial_conditions"):
+        cfg[k] = rec[k]
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64", "tubes": 64, "particles": n_all, "seed": args.seed,
-                       "tubes_on_rank0": len(tubes), "particles_on_rank0": n,
-                       "autotuned": dataclasses.asdict(choice),
-                       "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, ms=d) for a, b, c, d in log],
-                       "device_bytes": mem},
-            "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
-                                                                     phase)},
-            "gpu_launches": kps * args.steps, "clocks": clk}
+            "dtype": "f32", "data": "synthetic", "config": cfg,
+            "phase_ms_per_step": rec["phase_ms_per_step"], "gpu_launches": rec["gpu_launches"], "clocks": clk}
     print(json.dumps(line))
     return 0
 
 
 def run_serve(args):
-    """Poisson stream of uneven tubes, continuous batching under 150 GB."""
+    """Poisson stream of uneven tubes, continuous batching under 150 GB.
+
+    Comparators, all measured: the first --compare requests (by arrival, same
+    arrival times) served on their own, then solved one at a time in arrival
+    order on the FP32 path and on the plain FP64 path (ds_step of one tube per
+    context, a request waiting while the previous one runs)."""
     import numpy as np
 
     from dustyshock3d_gb300 import ic
-    from dustyshock3d_gb300.serve import Server, device_uneven_tube, poisson_requests
-    from dustyshock3d_gb300.solver import Solver
+    from dustyshock3d_gb300.serve import Server, device_uneven_tube, one_at_a_time, poisson_requests
     if args.host_ic:  # initial particles made on the host and uploaded at admission
         make = lambda rng: ic.uneven_tube(**ic.draw_tube_params(rng))  # noqa: E731
     else:  # generated on the device at admission (ds_init_tube)
         make = device_uneven_tube
     reqs = poisson_requests(args.rate, args.requests, args.seed, make)
+
+    def summary(res, wall, rebuilds=None, rebuild_s=None):
+        tts = np.array([r.time_to_solution for r in res])
+        ps = sum(r.particles * r.steps for r in res)
+        out = {"requests": len(res), "wall_s": wall, "particle_steps": ps, "value": ps / wall,
+               "p50_time_to_solution_s": float(np.percentile(tts, 50)),
+               "p99_time_to_solution_s": float(np.percentile(tts, 99))}
+        if rebuilds is not None:
+            out.update(rebuilds=rebuilds, rebuild_s=rebuild_s, rebuild_ms_each=1e3 * rebuild_s / max(rebuilds, 1))
+        return out
+
     clocks = ClockSampler(0)
     clocks.start()
     server = Server(budget_bytes=150e9, epoch_steps=10, precision="fp32")
     t0 = time.perf_counter()
     res = server.run(reqs)
     wall = time.perf_counter() - t0
+    full = summary(res, wall, server.rebuilds, server.rebuild_s)
+    comp = None
+    if args.compare > 0:
+        sub = sorted(reqs, key=lambda r: r.arrival)[:args.compare]
+        s2 = Server(budget_bytes=150e9, epoch_steps=10, precision="fp32")
+        t0 = time.perf_counter()
+        r2 = s2.run(sub)
+        served = summary(r2, time.perf_counter() - t0, s2.rebuilds, s2.rebuild_s)
+        rows = {"served_fp32": served}
+        for prec in ("fp32", "fp64"):
+            t0 = time.perf_counter()
+            rs = one_at_a_time(sub, prec)
+            rows[f"one_at_a_time_{prec}"] = summary(rs, time.perf_counter() - t0)
+        comp = {"subset": f"the first {len(sub)} requests by arrival ({sum(r.particles for r in sub)} particles), "
+                          "same arrival times", **rows}
     clk = clocks.stop()
-    tts = np.array([r.time_to_solution for r in res])
-    ps = sum(r.particles * r.steps for r in res)
-    # the same requests one at a time on the plain FP64 path: FP64 rate measured on
-    # the median-size request (a few steps), applied to every request's work
-    mid = sorted(reqs, key=lambda r: r.particles)[len(reqs) // 2]
-    P = mid.params.copy()
-    P.T_end = 1e9
-    with Solver(P) as S:
-        mid.put(S, 0)
-        S.step(2)
-        ms, _ = S.step_timed(3)
-    fp64_rate = mid.particles * 3 / (ms * 1e-3)
-    line = {"metric": "particle-steps/s", "value": ps / wall, "unit": "particle-steps/s", "n_gpus": 1,
+    line = {"metric": "particle-steps/s", "value": full["value"], "unit": "particle-steps/s", "n_gpus": 1,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "serve", "requests": len(reqs), "rate_per_s": args.rate, "seed": args.seed,
                        "budget_bytes": 150e9, "epoch_steps": 10, "t_end": "U[0.05, 0.2]",
                        "initial_conditions": "host" if args.host_ic else "device"},
-            "p50_time_to_solution_s": float(np.percentile(tts, 50)),
-            "p99_time_to_solution_s": float(np.percentile(tts, 99)), "wall_s": wall,
-            "rebuilds": server.rebuilds, "particle_steps": ps,
-            "one_at_a_time_fp64_estimate": {"rate": fp64_rate, "wall_s": ps / fp64_rate,
-                                            "sample": f"request {mid.rid} ({mid.particles} particles), 3 steps"},
-            "clocks": clk}
+            "p50_time_to_solution_s": full["p50_time_to_solution_s"],
+            "p99_time_to_solution_s": full["p99_time_to_solution_s"], "wall_s": full["wall_s"],
+            "rebuilds": full["rebuilds"], "rebuild_s": full["rebuild_s"], "rebuild_ms_each": full["rebuild_ms_each"],
+            "particle_steps": full["particle_steps"], "comparators": comp, "clocks": clk}
     print(json.dumps(line))
     return 0
 

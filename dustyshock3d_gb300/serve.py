@@ -127,6 +127,7 @@ class Server:
         self.precision = precision
         self.clock = clock
         self.rebuilds = 0
+        self.rebuild_s = 0.0  # wall time spent rebuilding the batch (new context, carried and new tubes)
         self.particle_steps = 0
 
     def _params(self, r: Request) -> Params:
@@ -183,6 +184,7 @@ class Server:
                 joined.append(r)
                 admitted_at[r.rid] = self.clock() - t0
             if joined or len(keep) != len(active):
+                rb0 = self.clock()
                 members = [r for _, r in keep] + joined
                 if members:
                     N = Solver([self._params(r) for r in members])
@@ -198,6 +200,7 @@ class Server:
                 S = N
                 active = members
                 self.rebuilds += 1
+                self.rebuild_s += self.clock() - rb0
             if S is None:
                 continue
             S.step(self.epoch_steps)
@@ -207,6 +210,33 @@ class Server:
         if S is not None:
             S.close()
         return sorted(results, key=lambda r: r.rid)
+
+
+def one_at_a_time(requests: List[Request], precision: str, clock: Callable[[], float] = time.perf_counter,
+                  group: int = 10) -> List[Result]:
+    """The same requests solved one at a time, in arrival order, each in its own
+    context (made, filled, stepped to its end time, read back, closed) as a
+    plain single-tube host would; a request that arrives while another runs
+    waits.  Measured in real time from the first arrival schedule, so the
+    time to solution includes the queueing a one-at-a-time service causes."""
+    results = []
+    t0 = clock()
+    for r in sorted(requests, key=lambda q: q.arrival):
+        wait = r.arrival - (clock() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        start = clock() - t0
+        P = r.params.copy()
+        P.T_end = r.t_end
+        P.precision = precision
+        with Solver(P) as S:
+            r.put(S, 0)
+            while S.time(0)[0] < r.t_end:
+                S.step(group)
+            nstep = S.time(0)[2]
+            sp = [S.get_species(0, s) for s in range(1 + P.n_dust)]
+        results.append(Result(r.rid, r.arrival, start, clock() - t0, nstep, r.particles, sp))
+    return sorted(results, key=lambda q: q.rid)
 
 
 def poisson_requests(rate_per_s: float, n: int, seed: int, make_tube, t_end_range=(0.05, 0.2)) -> List[Request]:

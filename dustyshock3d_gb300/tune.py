@@ -15,8 +15,9 @@ first ``sample`` tubes) with CUDA events and returns the fastest.
 from __future__ import annotations
 
 import dataclasses
-from typing import List, Sequence, Tuple
+from typing import List, Sequence, Tuple, Union
 
+from .ic import DeviceIC
 from .params import Params
 from .solver import Solver
 from .species import Species
@@ -58,8 +59,19 @@ def _fits(P: Params) -> bool:
     return True
 
 
-def tune(tubes: Sequence[Tuple[Params, List[Species]]], sample: int = 8, warmup: int = 2, steps: int = 3,
-         precision: str = "fp32", candidates=CANDIDATES) -> Tuple[Choice, list]:
+def put_tube(S: Solver, t: int, src) -> None:
+    """Tube t of S from host particles (a species list) or from a generator run
+    on the device (an ic.DeviceIC)."""
+    if isinstance(src, DeviceIC):
+        S.init_tube(t, src)
+    else:
+        S.set_tube(t, src)
+
+
+def tune(tubes: Sequence[Tuple[Params, Union[List[Species], DeviceIC]]], sample: int = 8, warmup: int = 2,
+         steps: int = 3, precision: str = "fp32", candidates=CANDIDATES) -> Tuple[Choice, list]:
+    """tubes: (params, particles) pairs, the particles a species list or a
+    DeviceIC generator."""
     sub = list(tubes[:sample])
     log = []
     best = None
@@ -72,7 +84,7 @@ def tune(tubes: Sequence[Tuple[Params, List[Species]]], sample: int = 8, warmup:
             continue
         with Solver(ps) as S:
             for t, (_, sp) in enumerate(sub):
-                S.set_tube(t, sp)
+                put_tube(S, t, sp)
             S.step(warmup)
             ms = S.step_timed_graph(steps)  # as ds_step runs the batch: its captured graphs
         ms /= steps

@@ -56,7 +56,8 @@ BOUNDS = {
                     plateau=0.32, fan_l1_v_gas=0.05),
 }
 # The FP32 path's L1 scores may exceed the FP64 path's by this factor (plus 1e-3).
-FP32_FACTOR = 1.25
+# Measured: FP32 / FP64 = 0.986 to 1.000 on every score of both cases.
+FP32_FACTOR = 1.05
 
 _runs = {}
 
@@ -106,7 +107,7 @@ def _run(name, engine):
     return res
 
 
-def _check_bounds(name, s, factor=1.0, ref=None):
+def _check_bounds(name, s, ref=None):
     b = BOUNDS[name]
     for k in ("l1_rho_gas", "l1_v_gas", "l1_v_dust", "l1_p_gas"):
         lim = b[k] if ref is None else FP32_FACTOR * ref[k] + 1e-3

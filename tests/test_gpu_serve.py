@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from dustyshock3d_gb300 import ic
-from dustyshock3d_gb300.serve import Request, Server, run_alone
+from dustyshock3d_gb300.serve import Request, Server, one_at_a_time, run_alone
 
 pytestmark = pytest.mark.gpu
 
@@ -72,3 +72,19 @@ def test_device_generated_requests_equal_uploaded_requests():
         for s in range(2):
             for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "ind"):
                 assert np.array_equal(getattr(ra.species[s], f), getattr(rb.species[s], f)), (ra.rid, s, f)
+
+
+def test_one_at_a_time_comparator_equals_the_served_results():
+    """The measured one-at-a-time comparator (serve.one_at_a_time) solves each
+    request alone, in arrival order: the same particles as the served mix, and
+    no request starts before the previous one finished."""
+    reqs = _requests()[:3]
+    served = Server(budget_bytes=150e9, epoch_steps=2, precision="fp32").run(reqs)
+    seq = one_at_a_time(reqs, "fp32", group=2)
+    for a, b in zip(served, seq):
+        assert a.rid == b.rid and a.steps == b.steps
+        for s in range(2):
+            assert np.array_equal(a.species[s].vx, b.species[s].vx) and np.array_equal(a.species[s].x, b.species[s].x)
+    order = sorted(seq, key=lambda r: r.arrival)
+    for x, y in zip(order, order[1:]):
+        assert y.admitted >= x.finished - 1e-9 and y.admitted >= y.arrival - 1e-9
