@@ -58,10 +58,16 @@ def _eq_state1(p, e, type_of_state, gam, cs):
     return p / (e * (gam - 1))
 
 
-def _reference_lattices(P: Params, e_lr, p_lr, rho_lr, cube, inner) -> Species:
+def _reference_lattices(P: Params, e_lr, p_lr, rho_lr, cube, inner, before_first: str = "error") -> Species:
     """The gas of the reference's two-lattice generators (kernel.cu:938-1042,
     1391-1495): left lattice x = 0 - i dl, right x = dl + i dl, points accepted
-    in ``cube``, Ind from the ``inner`` thresholds with the reference's quirk."""
+    in ``cube``, Ind from the ``inner`` thresholds with the reference's quirk.
+
+    before_first: lattice points before the first accepted one make the
+    reference write Ind_gas[-1], outside its array (kernel.cu:1441-1448;
+    undefined behaviour).  "error" refuses such a box; "skip" drops those
+    writes, which change no particle -- the reference's own default Init.txt
+    (a box of [-2, 2]^3 around the accept cube) is such a box."""
     h = P.h
     mas_particle = 1.0 / (P.Particle_on_length * P.Particle_on_length * P.Particle_on_length)
     dlh = [math.pow(mas_particle / rho_lr[0], 1 / 3.0), math.pow(mas_particle / rho_lr[1], 1 / 3.0)]
@@ -87,8 +93,11 @@ def _reference_lattices(P: Params, e_lr, p_lr, rho_lr, cube, inner) -> Species:
     interior = (np.abs(X) <= inner[0]) & (np.abs(Y) <= inner[1]) & (np.abs(Z) <= inner[2])
     pidx = np.cumsum(acc) - 1  # index of the last accepted particle at each lattice point
     if len(pidx) and pidx[0] < 0:
-        raise ValueError("first lattice point rejected: the reference writes Ind_gas[-1] here "
-                         "(undefined behaviour); choose Y_min, Z_min inside the accept cube")
+        if before_first != "skip":
+            raise ValueError("first lattice point rejected: the reference writes Ind_gas[-1] here "
+                             "(undefined behaviour); choose Y_min, Z_min inside the accept cube")
+        keep = pidx >= 0
+        pidx, interior = pidx[keep], interior[keep]
     N = int(acc.sum())
     if N > P.Maximum_particle:
         raise ValueError(f"{N} gas particles exceed Maximum_particle={P.Maximum_particle} "
@@ -123,9 +132,11 @@ def _dust_on_gas(P: Params, gas: Species) -> List[Species]:
     return dust
 
 
-def init_sod_x_dust(P: Params) -> Tuple[Params, List[Species]]:
+def init_sod_x_dust(P: Params, before_first: str = "error") -> Tuple[Params, List[Species]]:
     """kernel.cu:1391-1582: gas on two lattices (e 2.5 | 2.0, rho 1 | 1) and two
-    dust species copied onto the gas positions.  Returns (params, [gas, d1, d2])."""
+    dust species copied onto the gas positions.  Returns (params, [gas, d1, d2]).
+    before_first: see _reference_lattices ("skip" runs the reference's default
+    Init.txt box)."""
     P = P.copy()
     border_length = 2.5 * P.h
     X_cube, Y_cube, Z_cube = 1.0, 0.8, 0.8
@@ -133,7 +144,7 @@ def init_sod_x_dust(P: Params) -> Tuple[Params, List[Species]]:
     p_lr = tuple(_eq_state(rho_lr[s], e_lr[s], P.Type_of_state, 1.4, 1.0) for s in range(2))
     # the interior test compares |y| with X_cube (kernel.cu:1441, 1481)
     inner = (X_cube - border_length, X_cube - border_length, Z_cube - border_length)
-    gas = _reference_lattices(P, e_lr, p_lr, rho_lr, (X_cube, Y_cube, Z_cube), inner)
+    gas = _reference_lattices(P, e_lr, p_lr, rho_lr, (X_cube, Y_cube, Z_cube), inner, before_first)
     # kernel.cu:1497-1502
     P.Coeff_h_dust_cell = 0.5
     P.n_dust = 2
