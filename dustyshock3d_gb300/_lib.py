@@ -36,6 +36,7 @@ class DsParams(ctypes.Structure):
         ("t_empty", ctypes.c_double), ("list_depth", ctypes.c_int), ("force_list", ctypes.c_int),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
         ("t_stop_const", ctypes.c_double * MAX_DUST), ("eps_empty", ctypes.c_double * MAX_DUST),
+        ("list_skin", ctypes.c_double),
     ]
 
 
@@ -92,6 +93,9 @@ SIGNATURES = {
     "ds_load_tube": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
     "ds_memory_bytes": ([_VP, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "ds_last_error": ([_VP, _IP, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+    "ds_list_stats": ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+                      ctypes.c_int),
+    "ds_debug_force_lists": ([_VP, ctypes.c_int, ctypes.c_int, _IP, _IP], ctypes.c_int),
     "ds_cell_lists_noalloc": ([ctypes.POINTER(DsParams), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                                _VP, _VP], ctypes.c_int),
     "ds_host_alloc": ([ctypes.POINTER(_VP), ctypes.c_longlong], ctypes.c_int),
@@ -143,6 +147,7 @@ def params_to_c(P: Params) -> DsParams:
     c.stencil = int(getattr(P, "stencil", 1) or 1)
     c.list_depth = int(getattr(P, "list_depth", 0) or 0)
     c.force_list = int(getattr(P, "force_list", 0) or 0)
+    c.list_skin = float(getattr(P, "list_skin", 0.0) or 0.0)
     for k in range(MAX_DUST):
         c.mass_ratio[k] = float(P.mass_ratio[k]) if k < len(P.mass_ratio) else 0.0
         c.R_dust[k] = float(P.R_dust[k]) if k < len(P.R_dust) else 0.0
@@ -167,6 +172,7 @@ def params_from_c(c: DsParams) -> Params:
     P.stencil = int(c.stencil)
     P.list_depth = int(c.list_depth)
     P.force_list = int(c.force_list)
+    P.list_skin = float(c.list_skin)
     P.mass_ratio = [float(c.mass_ratio[k]) for k in range(P.n_dust)]
     P.R_dust = [float(c.R_dust[k]) for k in range(P.n_dust)]
     P.t_stop_const = [float(c.t_stop_const[k]) for k in range(P.n_dust)]

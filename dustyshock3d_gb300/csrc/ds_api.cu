@@ -103,6 +103,12 @@ struct ds_ctx {
   int *nbl_cnt = nullptr;
   unsigned char *nbl_walk = nullptr;
   int nbl_cap = 0;
+  // list reuse (some tube with a skin): FP32 offsets at each tube's last
+  // re-sort, displacements, per-key statistics, and the device flags of the
+  // start-of-step test (force: every tube re-sorts; any: some tube re-sorts)
+  bool reuse = false;
+  float4 *pos_ref = nullptr, *disp = nullptr, *cellstat = nullptr;
+  int *d_force = nullptr, *d_any = nullptr;
   uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
   uint32_t *ikin = nullptr, *ivin = nullptr, *ikalt = nullptr, *ivalt = nullptr;
   uint32_t *rs_scratch = nullptr;
@@ -209,7 +215,14 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   memset(&T, 0, sizeof(T));
   T.mode = P.mode;
   T.ox = P.X_min; T.oy = P.Y_min; T.oz = P.Z_min;
-  const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;
+  const bool proper = (P.mode & DS_MODE_GRID_PROPER) != 0;
+  // list reuse (FP32 path with force lists): record 2 max(h_i, h_j) + skin and
+  // widen the cells so that the stencil's cells still cover that cut-off
+  const bool reuse = P.list_skin > 0 && P.precision == DS_PRECISION_FP32 && P.force_list != -1 && proper &&
+                     !(P.mode & DS_MODE_DUST_RHO);
+  T.skin = reuse ? P.list_skin * P.h : 0.0;
+  const int nst = proper && P.stencil > 1 ? P.stencil : 1;
+  const double w = (P.cell_w > 0 ? P.cell_w : 2.0 * P.h) + T.skin / nst;
   T.Cnx = (int)((P.X_max - P.X_min) / w);
   T.Cny = (int)((P.Y_max - P.Y_min) / w);
   T.Cnz = (int)((P.Z_max - P.Z_min) / w);
@@ -217,7 +230,6 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   T.Lz = P.Z_max - P.Z_min;
   T.ymax = P.Y_max; T.zmax = P.Z_max;
   T.wx = T.wy = T.wz = w;
-  const bool proper = (P.mode & DS_MODE_GRID_PROPER) != 0;
   if (!proper) {
     T.sy = T.Cnx;
     T.sz = T.Cnx * T.Cny;
@@ -268,7 +280,7 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   const double wmin = fmin(T.wx, fmin(T.wy, T.wz));
   T.r1_hmax = T.stencil >= 2 ? 0.5 * wmin * (1.0 - 1e-9) : 1e300;
   T.rw = 1.0 / (wmin * (1.0 - 1e-9));
-  T.reach_hmax = proper ? 0.5 * T.stencil * wmin * (1.0 + 1e-9) : 1e300;
+  T.reach_hmax = proper ? 0.5 * (T.stencil * wmin - T.skin) * (1.0 + 1e-9) : 1e300;
   T.inv_wx = 1.0 / T.wx; T.inv_wy = 1.0 / T.wy; T.inv_wz = 1.0 / T.wz; T.inv_aw = 1.0 / T.aw;
   set_index_maps(T);
 }
@@ -283,8 +295,9 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
     return fail(c, DS_ERR_UNSUPPORTED, "the fp32 path needs the proper cell grid (DS_MODE_GRID_PROPER)");
   if (((P.mode & (DS_MODE_PERIODIC_Y | DS_MODE_PERIODIC_Z)) != 0) && !(P.mode & DS_MODE_GRID_PROPER))
     return fail(c, DS_ERR_UNSUPPORTED, "periodic axes need the proper cell grid (DS_MODE_GRID_PROPER)");
+  if (!(P.list_skin >= 0 && P.list_skin <= 4)) return fail(c, DS_ERR_ARG, "list_skin must be in [0, 4]");
   {  // the grid sizes in double first: the int conversions and products of build_desc must not overflow
-    const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;
+    const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;  // list reuse only widens it: fewer cells
     const double aw = P.idic_w > 0 ? P.idic_w : P.Coeff_h_dust_cell * P.h;
     if (!(w > 0) || !(aw > 0) || !std::isfinite(w) || !std::isfinite(aw))
       return fail(c, DS_ERR_ARG, "cell widths must be positive and finite");
@@ -355,32 +368,47 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.nbl_cnt = nullptr;
   a.nbl_walk = nullptr;
   a.nbl_cap = 0;
+  a.reuse = 0;
   return a;
+}
+
+// The sorted keys' buffer of the FP32 path's sorts (a fixed number of passes).
+const uint32_t *fast_skey(const ds_ctx *c) {
+  return (ds_radix_passes(c->key_bits + c->xl) & 1) ? c->kalt : c->kin;
 }
 
 // Sort + reorder + cell ranges for the particles' current positions; flips
 // parity.  exact_order: cells list their particles in caller-index order even
-// on the FP32 path (the parity hook's lists).
-void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorder = nullptr) {
+// on the FP32 path (the parity hook's lists).  reuse: the step's list-reuse
+// decisions apply (TubeState::rebuild, set by the start-of-step test); any
+// other sort of a list-reuse context re-orders every tube, so the next step
+// must re-sort and record (the force flag).
+void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorder = nullptr, bool reuse = false) {
   cudaStream_t s = c->stream;
   DevState src = c->buf[c->parity].view();
   DevState dst = c->buf[c->parity ^ 1].view();
   const bool fast = c->any_fp32 && !exact_order;
   const int xl = fast ? c->xl : 0;  // fast keys carry the x bin below the cell
+  const bool ru = reuse && c->reuse && fast;
+  const TubeState *rts = ru ? c->d_tstate : nullptr;
+  const int *run_if = ru ? c->d_any : nullptr;
   c->last_xl = xl;
-  ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s);
+  ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s, rts,
+                 ru ? fast_skey(c) : nullptr);
   bool alt = false;
-  ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt);
+  ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt, run_if);
   const uint32_t *skey = alt ? c->kalt : c->kin;
   const uint32_t *sval = alt ? c->valt : c->vin;
   if (before_reorder) cudaStreamWaitEvent(s, before_reorder, 0);  // fields still arriving from the host
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
-                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, c->d_flags, fast, s);
-  ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s);
+                    c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, c->d_flags, fast, s, rts,
+                    (c->reuse && fast) ? c->pos_ref : nullptr);
+  ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s, run_if);
   c->skey = skey;
   if (c->any_stencil2)
     ds_launch_cell_radius(c->d_tubes, c->cell_start, c->nkeys, xl, dst.h, c->cwa, c->cwb, c->d_nseg_key0, c->d_nseg_tube,
-                          c->d_nseg_species, c->nnseg, c->krad, s);
+                          c->d_nseg_species, c->nnseg, c->krad, s, run_if);
+  if (c->reuse && !ru) cudaMemsetAsync(c->d_force, 1, sizeof(int), s);
   c->parity ^= 1;
 }
 
@@ -399,10 +427,12 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
     ag.nbl_cnt = c->nbl_cnt;
     ag.nbl_walk = c->nbl_walk;
     ag.nbl_cap = c->nbl_cap;
+    ag.reuse = c->reuse ? 1 : 0;
   }
   const int depth = c->params[0].list_depth;
   if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
+  if (fp32 && c->reuse) ds_launch_density32_lst(ag, c->any_hpp, s);  // tubes keeping their lists
   if (c->any_dust_rho) {
     if (fp32) ds_launch_density32(ad, c->any_hpp, 1, depth, s);
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
@@ -441,7 +471,12 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
 void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[0], c->stream);
   ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->stream);
-  enqueue_sort(c);
+  if (c->reuse)  // which tubes keep their lists this step
+    ds_launch_list_test(c->d_tubes, c->d_tstate, c->ntubes, c->d_ch_gas, (int)c->ch_gas.size(),
+                        c->buf[c->parity].view(), fast_skey(c), c->pos_ref, c->disp, c->d_nseg_key0, c->d_nseg_tube,
+                        c->d_nseg_species, c->nnseg, c->nkeys, c->cell_start, c->xl, c->krad, c->cellstat,
+                        c->d_force, c->d_any, c->stream);
+  enqueue_sort(c, false, nullptr, true);
   enqueue_physics(c, ev);
   if (ev) cudaEventRecord(ev[4], c->stream);
 }
@@ -553,7 +588,8 @@ void enqueue_bound_step(ds_ctx *c) {
   cudaEventRecord(c->e_up, s2);
   c->parity = P0 ^ 1;  // the caller-order state; the sort brings it back to P0
   ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, s);
-  enqueue_sort(c, false, c->e_up);
+  enqueue_sort(c, false, c->e_up);  // the host's arrays: every tube re-sorts
+  if (c->reuse) ds_launch_list_decide(c->d_tubes, c->d_tstate, c->ntubes, c->d_force, c->d_any, s);
   k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->buf[c->parity].pid, c->inv);
   enqueue_physics(c, nullptr, c->e_dens, c->e_force);
   DevState st = c->buf[c->parity].view();
@@ -666,6 +702,13 @@ ds_status finalize(ds_ctx *c) {
     CK(cudaStreamCreateWithFlags(&c->wstream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->e_wjoin, cudaEventDisableTiming));
+    for (const auto &T : c->tdesc) c->reuse = c->reuse || T.skin > 0.0;
+  }
+  if (c->reuse) {
+    DA(c->pos_ref, N); DA(c->disp, N); DA(c->cellstat, (size_t)nkeys);
+    DA(c->d_force, 1); DA(c->d_any, 1);
+    CK(cudaMemsetAsync(c->d_force, 1, sizeof(int), c->stream));  // the first step sorts and records
+    CK(cudaMemsetAsync(c->d_any, 1, sizeof(int), c->stream));
   }
   DA(c->d_cons, 8);
   DA(c->d_flags, 1);
@@ -894,6 +937,7 @@ ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fi
     if (all && dind) {
       k_upload_mapped<<<(n + 255) / 256, 256, 0, c->stream>>>(hf, dind, n, c->params[tube].h, B.view(), b);
       CK(cudaGetLastError());
+      if (c->reuse) CK(cudaMemsetAsync(c->d_force, 1, sizeof(int), c->stream));  // caller order: re-sort
       return DS_OK;
     }
   }
@@ -910,6 +954,7 @@ ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fi
   CK(cudaMemcpyAsync(B.ind + b, ind, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
   ds_launch_iota(B.pid + b, n, c->stream);  // caller order: slot b + p holds particle p
   CK(cudaGetLastError());
+  if (c->reuse) CK(cudaMemsetAsync(c->d_force, 1, sizeof(int), c->stream));  // the next step re-sorts
   CK(cudaStreamSynchronize(c->stream));
   return DS_OK;
 }
@@ -1190,6 +1235,7 @@ ds_status ds_init_tube(ds_ctx *c, int tube, const ds_ic *ic) {
     ds_launch_ic(*plan, s, c->buf[c->parity].view(), T.seg_begin[s], c->stream);
     CK(cudaGetLastError());
   }
+  if (c->reuse) CK(cudaMemsetAsync(c->d_force, 1, sizeof(int), c->stream));  // the next step re-sorts
   CK(cudaStreamSynchronize(c->stream));
   return DS_OK;
 }
@@ -1385,8 +1431,51 @@ ds_status ds_kernels_per_step(ds_ctx *c, int *count) {
   if (st != DS_OK) return st;
   // step_begin, keys, reorder, cell_start, density, t_stop, dt, force,
   // idic_reduce, idic_solve, relax_move, step_end, 3 per radix pass, dust density
+  // list reuse: displacements, cell statistics, bound, decision, density stream
   *count = 13 + 3 * (ds_radix_passes(c->key_bits + c->xl) + ds_radix_passes(c->ikey_bits)) + (c->any_dust_rho ? 1 : 0) +
-           (c->any_stencil2 ? 4 : 0) + (c->nbl ? 1 : 0);
+           (c->any_stencil2 ? 4 : 0) + (c->nbl ? 1 : 0) + (c->reuse ? 5 : 0);
+  return DS_OK;
+}
+
+ds_status ds_list_stats(ds_ctx *c, int tube, long long *rebuilds, long long *steps) {
+  if (!c || tube < 0 || tube >= c->ntubes) return DS_ERR_ARG;
+  if (!c->finalized) {
+    if (rebuilds) *rebuilds = 0;
+    if (steps) *steps = 0;
+    return DS_OK;
+  }
+  TubeState ts;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(&ts, c->d_tstate + tube, sizeof(ts), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (rebuilds) *rebuilds = c->reuse ? ts.nrebuild : ts.nstep;  // without reuse every step re-sorts
+  if (steps) *steps = ts.nstep;
+  return DS_OK;
+}
+
+ds_status ds_debug_force_lists(ds_ctx *c, int tube, int cap, int *count, int *nbr) {
+  if (!c || tube < 0 || tube >= c->ntubes || cap < 0 || !count || (cap > 0 && !nbr)) return DS_ERR_ARG;
+  if (!c->finalized) return fail(c, DS_ERR_STATE, "no resident state yet (call ds_step first)");
+  if (!c->nbl) return fail(c, DS_ERR_UNSUPPORTED, "no recorded force lists (FP32 path with force lists only)");
+  CK(cudaSetDevice(c->device));
+  const TubeDesc &T = c->tdesc[tube];
+  const int n = T.seg_end[0] - T.seg_begin[0];
+  if (n == 0) return DS_OK;
+  ScratchDev tmp;
+  int *dc = nullptr, *dn = nullptr;
+  CK(tmp.alloc(&dc, (size_t)n));
+  if (cap > 0) CK(tmp.alloc(&dn, (size_t)n * (size_t)cap));
+  CK(cudaMemsetAsync(dc, 0, sizeof(int) * (size_t)n, c->stream));
+  SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
+  ag.nbl = c->nbl;
+  ag.nbl_cnt = c->nbl_cnt;
+  ag.nbl_walk = c->nbl_walk;
+  ag.nbl_cap = c->nbl_cap;
+  ds_launch_debug_force_lists(ag, tube, cap, dc, dn, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(count, dc, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  if (cap > 0) CK(cudaMemcpyAsync(nbr, dn, sizeof(int) * (size_t)n * (size_t)cap, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return DS_OK;
 }
 
@@ -1475,7 +1564,7 @@ ds_status ds_save_tube(ds_ctx *c, int tube, const char *path) {
 // the tube's, by name, or nullptr.  Compared: everything that changes the
 // physics, the grids or the step (box, equation of state, h, cell widths,
 // fixed step, AV constants, gamma, sound speed, species and their constants,
-// mode bits, precision, stencil, CFL number, empty-cell defaults).  Not
+// mode bits, precision, stencil, CFL number, empty-cell defaults, list skin).  Not
 // compared: T_end and T_out (a resumed run may go further), Maximum_particle
 // and Particle_on_length (initial conditions only), list_depth and force_list
 // (tuning choices that leave the results unchanged).
@@ -1486,7 +1575,7 @@ static const char *checkpoint_param_mismatch(const ds_params &a, const ds_params
   DS_CK_FIELD(Z_max) DS_CK_FIELD(Type_of_state) DS_CK_FIELD(h) DS_CK_FIELD(Coeff_h_dust_cell) DS_CK_FIELD(tau)
   DS_CK_FIELD(alpha) DS_CK_FIELD(beta) DS_CK_FIELD(eps) DS_CK_FIELD(Gam_g) DS_CK_FIELD(Speed_of_sound_gas)
   DS_CK_FIELD(n_dust) DS_CK_FIELD(mode) DS_CK_FIELD(precision) DS_CK_FIELD(stencil) DS_CK_FIELD(cell_w)
-  DS_CK_FIELD(idic_w) DS_CK_FIELD(cfl) DS_CK_FIELD(t_empty)
+  DS_CK_FIELD(idic_w) DS_CK_FIELD(cfl) DS_CK_FIELD(t_empty) DS_CK_FIELD(list_skin)
   for (int k = 0; k < DS_MAX_DUST && k < a.n_dust; k++) {
     DS_CK_FIELD(mass_ratio[k]) DS_CK_FIELD(R_dust[k]) DS_CK_FIELD(t_stop_const[k]) DS_CK_FIELD(eps_empty[k])
   }

@@ -62,13 +62,23 @@ __device__ __forceinline__ int fast_idic_cell(const TubeDesc &T, double x, doubl
 // order: written at the particle's caller index, so the stable sort keeps
 // ascending index within a cell as the reference's lists do.  FP32 path:
 // written in slot order (coalesced); a cell then keeps its previous order.
+//
+// List reuse (ts != nullptr): a tube that keeps its recorded lists this step
+// keeps its slot order.  Its slots get the keys of the last sort (prev, the
+// sort's output of the previous step, slot by slot) with their own slot as the
+// value, so the stable sort leaves them where they are.
 template <bool FAST>
 __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                       uint32_t *vin) {
+                       uint32_t *vin, const TubeState *ts, const uint32_t *prev) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int i = ch.begin + threadIdx.x;
     if (i >= ch.end) continue;
+    if (FAST && ts && !ts[ch.tube].rebuild) {
+      kin[i] = prev[i];
+      vin[i] = (uint32_t)i;
+      continue;
+    }
     const TubeDesc &T = tubes[ch.tube];
     int local;
     uint32_t bin = 0;
@@ -99,17 +109,24 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
 // sorted order (dst); build the FP32 copies and the IDIC keys (reference
 // order: at the caller index, so the IDIC sums run in ascending index as the
 // reference's host loops do; FP32 path: in slot order).
+//
+// List reuse (ts != nullptr): a tube keeping its lists is copied slot for slot
+// (its order did not change), and its FP32 offsets stay relative to the cells
+// the lists were recorded in (its keys are those of the last sort), taken to
+// the nearest periodic image.  A tube that re-sorts stores its new offsets in
+// pos_ref, the reference its later displacements are measured from.
 template <bool FAST>
 __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                           const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32,
                           int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid,
-                          int *flags) {
+                          int *flags, const TubeState *ts, float4 *pos_ref) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int q = ch.begin + threadIdx.x;
     if (q >= ch.end) continue;
     const TubeDesc &T = tubes[ch.tube];
-    const int j = (int)order[q];
+    const bool keep = FAST && ts && !ts[ch.tube].rebuild;
+    const int j = keep ? q : (int)order[q];
     const double x = src.x[j], y = src.y[j], z = src.z[j];
     dst.x[q] = x; dst.y[q] = y; dst.z[q] = z;
     const double vx = src.vx[j], vy = src.vy[j], vz = src.vz[j];
@@ -150,8 +167,13 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
       const int bx = FAST ? ((ix >> DS_XB_LOG) << DS_XB_LOG) : ix;
       if (FAST && local < T.ncells) {
         p4.x = ds_d2f(x - T.orig[ix >> DS_XB_LOG]);
-        p4.y = ds_d2f(y - T.orig[T.nbx + iy]);
-        p4.z = ds_d2f(z - T.orig[T.nbx + T.ny + iz]);
+        double dy = y - T.orig[T.nbx + iy], dz = z - T.orig[T.nbx + T.ny + iz];
+        if (keep) {  // a kept particle may have wrapped through a periodic face since its cell was set
+          if (T.mode & M_PER_Y) dy += dy > 0.5 * T.Ly ? -T.Ly : (dy < -0.5 * T.Ly ? T.Ly : 0.0);
+          if (T.mode & M_PER_Z) dz += dz > 0.5 * T.Lz ? -T.Lz : (dz < -0.5 * T.Lz ? T.Lz : 0.0);
+        }
+        p4.y = ds_d2f(dy);
+        p4.z = ds_d2f(dz);
       } else {
         p4.x = ds_d2f(x - (T.ox + bx * T.wx));
         p4.y = ds_d2f(y - (T.oy + iy * T.wy));
@@ -165,6 +187,7 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     // FP32 copies converted on the integer pipe (ds_d2f: the IEEE conversion)
     p4.w = ds_d2f(h);
     pos32[q] = p4;
+    if (pos_ref && !keep) pos_ref[q] = p4;
     vm32[q] = make_float4(ds_d2f(vx), ds_d2f(vy), ds_d2f(vz), ds_d2f(m));
     const int ic = FAST ? fast_idic_cell(T, x, y, z) : ds_idic_cell(T, x, y, z);
     idic_local[q] = ic;
@@ -175,7 +198,10 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
 }
 
 // cell_start[k] = first sorted slot whose key is >= k, for k = 0..nkeys.
-__global__ void k_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start) {
+// run_if: skipped when *run_if == 0 (list reuse: no tube re-sorted, so the
+// keys and their table are those of the last sort).
+__global__ void k_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, const int *run_if) {
+  if (run_if && *run_if == 0) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q > n) return;
   const long long prev = q > 0 ? (long long)skey[q - 1] : -1LL;
@@ -734,7 +760,9 @@ __global__ void k_debug_lists(const TubeDesc *tubes, int tube, int s, DevState s
 // its maximum over the x window, the y window, then the z window (periodic
 // axes wrap).  Reference grids and the orphan buckets keep the tube's stencil;
 // tubes without per-particle h (every cut-off 2 h of the run) take its radius.
-__global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const double *h, double *hmax) {
+__global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const double *h, double *hmax,
+                            const int *run_if) {
+  if (run_if && *run_if == 0) return;
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
   // maximum as bit patterns (integer pipe): the same value as fmax for h >= 0
@@ -750,7 +778,8 @@ __global__ void k_cell_hmax(const int *cell_start, int nkeys, int xl, const doub
 template <int AXIS>
 __global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const int *nseg_tube,
                               const int *nseg_species, int nseg, int nkeys, const double *in, double *out,
-                              unsigned char *krad) {
+                              unsigned char *krad, const int *run_if) {
+  if (run_if && *run_if == 0) return;
   const int key = blockIdx.x * blockDim.x + threadIdx.x;
   if (key >= nkeys) return;
   const int sg = find_seg(nseg_key0, nseg, key);
@@ -764,7 +793,7 @@ __global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const
     return;
   }
   if (!(T.mode & M_HPP)) {  // one h for every pair (the run's h, not the h field): one radius
-    if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * T.h);
+    if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * T.h + T.skin);
     return;
   }
   const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
@@ -788,7 +817,7 @@ __global__ void k_cell_window(const TubeDesc *tubes, const int *nseg_key0, const
     }
     m = fmax(m, in[c]);
   }
-  if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * m);
+  if (AXIS == 2) krad[key] = (unsigned char)ds_radius(T, 2.0 * m + T.skin);  // the recorded cut-off
   else out[key] = m;
 }
 
@@ -800,6 +829,236 @@ __global__ void k_origins(double ox, double wx, int nbx, double oy, double wy, i
   if (i < nbx) orig[i] = ox + (i * DS_XB) * wx;
   else if (i < nbx + ny) orig[i] = oy + (i - nbx) * wy;
   else if (i < nbx + ny + nz) orig[i] = oz + (i - nbx - ny) * wz;
+}
+
+// ---------------------------------------------------------------------------
+// List reuse: the test, at the start of a step, of whether a tube's recorded
+// lists still hold every pair within its cut-off.  The lists of particle i
+// hold every j with |x0_i - x0_j| < rc_ij = 2 max(h_i, h_j) + skin (x0: the
+// positions when they were recorded).  With d the displacements since then, a
+// pair now within 2 max(h_i, h_j) that is not listed has |d_i - d_j| > skin.
+// Per cell c of the recording sort: m_c, the mean displacement of its
+// particles, and dev_c, the largest |d_i - m_c| in it.  For i in c, j in c',
+// |d_i - d_j| <= dev_c + dev_c' + |m_c - m_c'| (the triangle inequality).
+//   * c' within r_c + 1 cells of c (r_c: the cells the recording walk of c
+//     searched, r_c w >= rc_ij, w the least cell width): the tube keeps its
+//     lists only while dev_c + dev_c' + |m_c - m_c'| < skin for all of them.
+//   * c' further (along some axis more than r_c + 1 cells): the pair was more
+//     than (r_c + 1) w >= rc_ij + w apart, so it is within its cut-off now
+//     only if |d_i - d_j| > skin + w; bounded by 2 G + |M|, G the tube's
+//     largest dev_c and |M| the diagonal of the box holding every m_c.  The
+//     tube keeps its lists only while 2 G + |M| < skin + w.
+// A particle outside the grid (its own bucket, no cell) makes its tube
+// re-sort every step.  The values are the FP32 offsets the screens use; the
+// decision keeps 0.1 % of each threshold for their rounding.
+// ---------------------------------------------------------------------------
+
+// order-preserving map of a float to an unsigned (for atomicMin / atomicMax)
+__device__ __forceinline__ unsigned ord_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ord_float(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Combine v into *p with one atomic per group of lanes naming the same p
+// (p == nullptr: nothing).  Every lane of the warp calls it.
+__device__ __forceinline__ void warp_atomic_max(unsigned *p, unsigned v) {
+  const unsigned grp = __match_any_sync(0xffffffffu, (unsigned long long)p);
+  const unsigned m = __reduce_max_sync(grp, v);
+  if (p && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(p, m);
+}
+__device__ __forceinline__ void warp_atomic_min(unsigned *p, unsigned v) {
+  const unsigned grp = __match_any_sync(0xffffffffu, (unsigned long long)p);
+  const unsigned m = __reduce_min_sync(grp, v);
+  if (p && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMin(p, m);
+}
+
+// the FP32 offset of a position from the cell (ix, iy, iz) of the FP32 path
+// (x from the cell's x-block origin), periodic axes to the nearest image
+__device__ __forceinline__ float4 list_offset(const TubeDesc &T, int ix, int iy, int iz, double x, double y, double z) {
+  double dy = y - T.orig[T.nbx + iy], dz = z - T.orig[T.nbx + T.ny + iz];
+  if (T.mode & M_PER_Y) dy += dy > 0.5 * T.Ly ? -T.Ly : (dy < -0.5 * T.Ly ? T.Ly : 0.0);
+  if (T.mode & M_PER_Z) dz += dz > 0.5 * T.Lz ? -T.Lz : (dz < -0.5 * T.Lz ? T.Lz : 0.0);
+  return make_float4(ds_d2f(x - T.orig[ix >> DS_XB_LOG]), ds_d2f(dy), ds_d2f(dz), 0.0f);
+}
+
+// displacement of every gas slot of a reusing tube since its lists were
+// recorded; a slot outside the grid marks its tube (re-sort)
+__global__ void k_list_disp(const TubeDesc *tubes, TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
+                            const uint32_t *skey, const float4 *pos_ref, float4 *disp, const int *force) {
+  if (*force) return;
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int q = ch.begin + threadIdx.x;
+    if (q >= ch.end) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    if (!(T.skin > 0.0) || !ts[ch.tube].built) continue;
+    const int local = (int)(skey[q] >> T.xl) - T.key_base[ch.species];
+    float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (local >= 0 && local < T.ncells) {
+      const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
+      const float4 o = list_offset(T, ix, iy, iz, st.x[q], st.y[q], st.z[q]);
+      const float4 r = pos_ref[q];
+      d = make_float4(o.x - r.x, o.y - r.y, o.z - r.z, 0.0f);
+    } else {
+      atomicMax(&ts[ch.tube].disp_bits, 0x7f800000u);  // +inf: re-sort
+    }
+    disp[q] = d;
+  }
+}
+
+// per gas cell of a reusing tube: mean displacement (xyz) and the largest
+// distance of a displacement from it (w; -1 for an empty cell); per tube the
+// largest of those distances and the box of the means
+__global__ void k_list_cellstat(const TubeDesc *tubes, TubeState *ts, const int *nseg_key0, const int *nseg_tube,
+                                const int *nseg_species, int nseg, int nkeys, const int *cell_start, int xl,
+                                const float4 *disp, float4 *stat, const int *force) {
+  if (*force) return;  // uniform over the grid
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  bool act = key < nkeys;
+  int t = 0;
+  if (act) {
+    const int sg = find_seg(nseg_key0, nseg, key);
+    t = nseg_tube[sg];
+    act = nseg_species[sg] == 0 && tubes[t].skin > 0.0 && ts[t].built && key - tubes[t].key_base[0] < tubes[t].ncells;
+  }
+  float4 out = make_float4(0.f, 0.f, 0.f, -1.f);
+  if (act) {
+    const int a = cell_start[key << xl], b = cell_start[(key + 1) << xl];
+    if (b > a) {
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      for (int j = a; j < b; j++) {
+        const float4 d = disp[j];
+        sx += d.x; sy += d.y; sz += d.z;
+      }
+      const float inv = 1.0f / (float)(b - a);
+      const float mx = sx * inv, my = sy * inv, mz = sz * inv;
+      float dev2 = 0.f;
+      bool bad = !(fabsf(mx) <= 3.0e38f && fabsf(my) <= 3.0e38f && fabsf(mz) <= 3.0e38f);
+      for (int j = a; j < b; j++) {
+        const float4 d = disp[j];
+        const float ex = d.x - mx, ey = d.y - my, ez = d.z - mz;
+        const float e2 = ex * ex + ey * ey + ez * ez;
+        bad |= !(e2 <= 3.0e38f);
+        dev2 = fmaxf(dev2, e2);
+      }
+      out = make_float4(mx, my, mz, bad ? __int_as_float(0x7f800000) : sqrtf(dev2));
+    }
+    stat[key] = out;
+  }
+  const bool full = act && out.w >= 0.0f;
+  TubeState *S = full ? ts + t : nullptr;
+  warp_atomic_max(S ? &S->gdev_bits : nullptr, full ? __float_as_uint(out.w) : 0u);
+  warp_atomic_min(S ? &S->mlo[0] : nullptr, full ? ord_bits(out.x) : 0xffffffffu);
+  warp_atomic_min(S ? &S->mlo[1] : nullptr, full ? ord_bits(out.y) : 0xffffffffu);
+  warp_atomic_min(S ? &S->mlo[2] : nullptr, full ? ord_bits(out.z) : 0xffffffffu);
+  warp_atomic_max(S ? &S->mhi[0] : nullptr, full ? ord_bits(out.x) : 0u);
+  warp_atomic_max(S ? &S->mhi[1] : nullptr, full ? ord_bits(out.y) : 0u);
+  warp_atomic_max(S ? &S->mhi[2] : nullptr, full ? ord_bits(out.z) : 0u);
+}
+
+// (c + k) mod n for any offset k, n >= 1
+__device__ __forceinline__ int wrap_index(int c, int n) {
+  c %= n;
+  return c < 0 ? c + n : c;
+}
+
+// per gas cell c of a reusing tube: the largest dev_c + dev_c' + |m_c - m_c'|
+// over the non-empty cells c' within r_c + 1 cells (each unordered pair once:
+// c' after c in the (z, y, x) order of the offsets), max-reduced per tube into
+// disp_bits (a float >= 0 as bits; not finite -> +inf)
+__global__ void k_list_bound(const TubeDesc *tubes, TubeState *ts, const int *nseg_key0, const int *nseg_tube,
+                             const int *nseg_species, int nseg, int nkeys, const unsigned char *krad,
+                             const float4 *stat, const int *force) {
+  if (*force) return;  // uniform over the grid
+  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  bool act = key < nkeys;
+  int t = 0;
+  if (act) {
+    const int sg = find_seg(nseg_key0, nseg, key);
+    t = nseg_tube[sg];
+    act = nseg_species[sg] == 0 && tubes[t].skin > 0.0 && ts[t].built && key - tubes[t].key_base[0] < tubes[t].ncells;
+  }
+  float m = 0.0f;
+  bool bad = false;
+  const float4 a = act ? stat[key] : make_float4(0.f, 0.f, 0.f, -1.f);
+  act = act && a.w >= 0.0f;
+  if (act) {
+    const TubeDesc &T = tubes[t];
+    const int kb = T.key_base[0];
+    const int local = key - kb;
+    const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
+    int r = T.stencil == 1 ? 1 : (int)krad[key];
+    r = (r < 1 ? 1 : (r > T.stencil ? T.stencil : r)) + 1;
+    m = 2.0f * a.w;  // two particles of the cell itself
+    bad = !(a.w <= 3.0e38f);
+    for (int g = 0; g <= r; g++) {
+      int cz = iz + g;
+      if (T.mode & M_PER_Z) cz = wrap_index(cz, T.nz);
+      else if (cz >= T.nz) break;
+      for (int l = g == 0 ? 0 : -r; l <= r; l++) {
+        int cy = iy + l;
+        if (T.mode & M_PER_Y) cy = wrap_index(cy, T.ny);
+        else if (cy < 0 || cy >= T.ny) continue;
+        for (int k = (g == 0 && l == 0) ? 1 : -r; k <= r; k++) {
+          const int cx = ix + k;
+          if (cx < 0 || cx >= T.nx) continue;
+          const float4 b = stat[kb + cx + cy * T.sy + cz * T.sz];
+          if (b.w < 0.0f) continue;
+          const float ex = a.x - b.x, ey = a.y - b.y, ez = a.z - b.z;
+          const float bound = a.w + b.w + sqrtf(ex * ex + ey * ey + ez * ez);
+          bad |= !(bound <= 3.0e38f);
+          m = fmaxf(m, bound);
+        }
+      }
+    }
+  }
+  warp_atomic_max(act ? &ts[t].disp_bits : nullptr, bad ? 0x7f800000u : __float_as_uint(m));
+}
+
+// per tube: re-sort and record this step, or keep the lists; *any: some tube
+// re-sorts (the sort and the cell tables run); *force: every tube re-sorts
+// (the state was replaced or re-ordered since the last step), then cleared.
+// Resets the tube's statistics for the next test.
+__global__ void k_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any) {
+  __shared__ int s_any;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  const int f = *force;
+  for (int t = threadIdx.x; t < ntubes; t += blockDim.x) {
+    const TubeDesc &T = tubes[t];
+    TubeState &S = ts[t];
+    int rb = 1;
+    if (T.skin > 0.0 && !f && S.built) {
+      const float skin = (float)T.skin;
+      const float wmin = (float)fmin(T.wx, fmin(T.wy, T.wz));
+      const float local = __uint_as_float(S.disp_bits);
+      float far = 2.0f * __uint_as_float(S.gdev_bits);
+      if (S.mhi[0] >= S.mlo[0]) {  // some cell has particles
+        const float ex = ord_float(S.mhi[0]) - ord_float(S.mlo[0]);
+        const float ey = ord_float(S.mhi[1]) - ord_float(S.mlo[1]);
+        const float ez = ord_float(S.mhi[2]) - ord_float(S.mlo[2]);
+        far += sqrtf(ex * ex + ey * ey + ez * ez);
+      }
+      rb = (local < 0.999f * skin && far < 0.999f * (skin + wmin)) ? 0 : 1;
+    }
+    S.rebuild = rb;
+    S.disp_bits = 0u;
+    S.gdev_bits = 0u;
+    for (int a = 0; a < 3; a++) { S.mlo[a] = 0xffffffffu; S.mhi[a] = 0u; }
+    if (rb) {
+      S.built = T.skin > 0.0 ? 1 : 0;
+      S.nrebuild++;
+      s_any = 1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *any = s_any;
+    *force = 0;
+  }
 }
 
 __global__ void k_fill(double *a, int n, double v) {
@@ -823,25 +1082,47 @@ void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cuda
   k_step_begin<<<blocks_for(ntubes, 64), 64, 0, s>>>(tubes, ts, ntubes);
 }
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                    uint32_t *vin, bool fast, cudaStream_t s) {
+                    uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts, const uint32_t *prev_skey) {
   if (!nchunks) return;
-  if (fast) k_keys<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
-  else k_keys<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin);
+  if (fast) k_keys<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, reuse_ts, prev_skey);
+  else k_keys<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, nullptr, nullptr);
 }
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
-                       cudaStream_t s) {
+                       cudaStream_t s, const TubeState *reuse_ts, float4 *pos_ref) {
   if (!nchunks) return;
   if (fast)
     k_reorder<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
-                                                 idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags);
+                                                 idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, reuse_ts,
+                                                 pos_ref);
   else
     k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
-                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags);
+                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, nullptr,
+                                                  nullptr);
 }
-void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s) {
-  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start);
+void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
+                          const int *run_if) {
+  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(skey, n, nkeys, cell_start, run_if);
+}
+void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const Chunk *gas_chunks,
+                         int ngas_chunks, DevState st, const uint32_t *skey, const float4 *pos_ref, float4 *disp,
+                         const int *nseg_key0, const int *nseg_tube, const int *nseg_species, int nseg, int nkeys,
+                         const int *cell_start, int xl, const unsigned char *krad, float4 *cellstat, int *force,
+                         int *any, cudaStream_t s) {
+  if (ngas_chunks)
+    k_list_disp<<<ngas_chunks, DS_CHUNK, 0, s>>>(tubes, ts, gas_chunks, ngas_chunks, st, skey, pos_ref, disp, force);
+  if (nkeys > 0) {
+    const int b = blocks_for(nkeys, 128);
+    k_list_cellstat<<<b, 128, 0, s>>>(tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, cell_start, xl,
+                                      disp, cellstat, force);
+    k_list_bound<<<b, 128, 0, s>>>(tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, krad, cellstat,
+                                   force);
+  }
+  k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);
+}
+void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s) {
+  k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);
 }
 #ifndef DS_IDIC_LANES
 #define DS_IDIC_LANES 4  // lanes per IDIC key of the FP32 path's cell sums (measured: 4 beats 8)
@@ -850,7 +1131,7 @@ void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, i
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
                            bool fast, cudaStream_t s) {
   if (nikeys <= 0) return;
-  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start);
+  k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start, nullptr);
   if (fast)
     k_idic_reduce_split<DS_IDIC_LANES><<<(int)(((long long)DS_IDIC_LANES * nikeys + 127) / 128), 128, 0, s>>>(
         islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca);
@@ -906,11 +1187,13 @@ void ds_launch_iota(int *a, int n, cudaStream_t s) {
 }
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, int xl, const double *h,
                            double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,
-                           const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s) {
+                           const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s,
+                           const int *run_if) {
   if (nkeys <= 0) return;
   const int b = blocks_for(nkeys, 256);
-  k_cell_hmax<<<b, 256, 0, s>>>(cell_start, nkeys, xl, h, wa);
-  k_cell_window<0><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, wb, krad);
-  k_cell_window<1><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wb, wa, krad);
-  k_cell_window<2><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, nullptr, krad);
+  k_cell_hmax<<<b, 256, 0, s>>>(cell_start, nkeys, xl, h, wa, run_if);
+  k_cell_window<0><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, wb, krad, run_if);
+  k_cell_window<1><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wb, wa, krad, run_if);
+  k_cell_window<2><<<b, 256, 0, s>>>(tubes, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, wa, nullptr, krad,
+                                     run_if);
 }

@@ -60,6 +60,7 @@ struct TubeDesc {
   double r1_hmax;    // particles and cells with h <= r1_hmax need only the 27 inner cells
   double reach_hmax; // proper grid: largest h whose cut-off 2h the stencil's cells cover
   double rw;         // 1 / (min cell width (1 - 1e-9)): a cut-off c needs ceil(c rw) cells per side
+  double skin;       // FP32 path, list reuse: recorded cut-off 2 max(h_i, h_j) + skin (0: lists rebuilt every step)
   double inv_wx, inv_wy, inv_wz, inv_aw;  // reciprocal cell widths (FP32 path: no FP64 divisions)
   // FP32 path index maps, one FMA and one rounding conversion per axis (GB300's
   // FP64 pipe runs 2 lanes per SM per clock): fine x index floor(fma(x, kxa,
@@ -81,7 +82,12 @@ struct TubeState {
   unsigned long long dtmin_bits;  // CFL min-reduction (bits of a positive double)
   long long nstep;
   int active;          // Tm < T_end at the start of the step
-  int pad;
+  int rebuild;         // list reuse: this step sorts, walks and records the lists (1 without reuse)
+  unsigned disp_bits;  // list reuse: largest bound over nearby cell pairs (bits of a float >= 0)
+  int built;           // list reuse: lists recorded since the context's state was last replaced
+  unsigned gdev_bits;  // list reuse: largest distance of a displacement from its cell's mean (float bits)
+  unsigned mlo[3], mhi[3];  // list reuse: box of the cells' mean displacements (order-preserving bits)
+  long long nrebuild;  // list reuse: steps that sorted and recorded
 };
 
 // A block-sized chunk of one segment: blocks of the per-phase kernels walk a
@@ -604,4 +610,7 @@ struct SweepArgs {
   int *nbl_cnt;                // entries per slot
   unsigned char *nbl_walk;     // per warp of each gas chunk: 1 when a particle overflowed (that warp walks)
   int nbl_cap;
+  // list reuse: a tube whose TubeState::rebuild is 0 this step keeps the lists
+  // (and slot order) of its last re-sort; 0: every step re-sorts and records
+  int reuse;
 };

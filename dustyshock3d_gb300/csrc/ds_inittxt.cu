@@ -146,7 +146,8 @@ ds_status apply_param_extension(ds_params *p, const std::string &key, const std:
                       {"h", &p->h}, {"Coeff_h_dust_cell", &p->Coeff_h_dust_cell}, {"tau", &p->tau},
                       {"T_end", &p->T_end}, {"T_out", &p->T_out}, {"alpha", &p->alpha}, {"beta", &p->beta},
                       {"eps", &p->eps}, {"Gam_g", &p->Gam_g}, {"Speed_of_sound_gas", &p->Speed_of_sound_gas},
-                      {"t_empty", &p->t_empty}, {"cell_w", &p->cell_w}, {"idic_w", &p->idic_w}, {"cfl", &p->cfl}};
+                      {"t_empty", &p->t_empty}, {"cell_w", &p->cell_w}, {"idic_w", &p->idic_w}, {"cfl", &p->cfl},
+                      {"list_skin", &p->list_skin}};
   for (const DName &d : dn)
     if (key == d.name) return parse_double(val, d.d) ? DS_OK : DS_ERR_ARG;
   if (key == "Type_of_state" || key == "Maximum_particle") {  // numbers, truncated to int

@@ -23,13 +23,29 @@ struct CellArrays {
 void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
 // fast: FP32 path (reciprocal-multiply cell indices, slot-order scatters);
 // otherwise the reference's divisions and caller-index order.
+// List reuse (FP32 path): reuse_ts != nullptr gives each tube's decision of the
+// step (TubeState::rebuild); a tube keeping its lists keeps its slot order:
+// prev_skey, the previous sort's keys, become its keys, and the reorder copies
+// it slot for slot.  pos_ref receives the FP32 offsets of re-sorted tubes.
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                    uint32_t *vin, bool fast, cudaStream_t s);
+                    uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts = nullptr,
+                    const uint32_t *prev_skey = nullptr);
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
-                       cudaStream_t s);
-void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s);
+                       cudaStream_t s, const TubeState *reuse_ts = nullptr, float4 *pos_ref = nullptr);
+// run_if: skipped when *run_if == 0 (no tube re-sorted this step)
+void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
+                          const int *run_if = nullptr);
+// List reuse: the start-of-step test (displacements, per-cell statistics, the
+// bound per tube) and the per-tube decision; *any = some tube re-sorts.
+void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const Chunk *gas_chunks,
+                         int ngas_chunks, DevState st, const uint32_t *skey, const float4 *pos_ref, float4 *disp,
+                         const int *nseg_key0, const int *nseg_tube, const int *nseg_species, int nseg, int nkeys,
+                         const int *cell_start, int xl, const unsigned char *krad, float4 *cellstat, int *force,
+                         int *any, cudaStream_t s);
+// the decision alone (with *force set: every tube re-sorts)
+void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s);
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
                            bool fast, cudaStream_t s);
@@ -49,7 +65,8 @@ void ds_launch_debug_lists(const TubeDesc *tubes, int tube, int species, int nse
 
 void ds_launch_cell_radius(const TubeDesc *tubes, const int *cell_start, int nkeys, int xl, const double *h,
                            double *wa, double *wb, const int *nseg_key0, const int *nseg_tube,
-                           const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s);
+                           const int *nseg_species, int nseg, unsigned char *krad, cudaStream_t s,
+                           const int *run_if = nullptr);
 void ds_launch_origins(const TubeDesc &T, double *orig, cudaStream_t s);
 void ds_launch_fill(double *a, int n, double v, cudaStream_t s);
 void ds_launch_iota(int *a, int n, cudaStream_t s);
@@ -63,3 +80,7 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
 void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);
 void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s);
 void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);
+// list reuse: the density of tubes keeping their lists, streamed from them
+void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s);
+// parity hook: one tube's recorded force lists by caller index (a: gas chunks)
+void ds_launch_debug_force_lists(const SweepArgs &a, int tube, int cap, int *count, int *nbr, cudaStream_t s);

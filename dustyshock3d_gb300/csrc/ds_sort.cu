@@ -35,8 +35,12 @@ constexpr int RS_BINS = 1 << RS_MAX_BITS;        // digit values at most
 static_assert(RS_BINS <= DS_RADIX_BINS, "histogram rows are sized for DS_RADIX_BINS digit values");
 constexpr int RS_DPT = RS_BINS / RS_THREADS;     // digit values per thread in the scatter's scan
 
+// run_if (all three kernels): nullptr, or the sort is skipped when *run_if == 0
+// (the whole grid returns at once, before any barrier).
 __global__ void __launch_bounds__(RS_THREADS) rs_hist(const uint32_t *__restrict__ keys, int n, int shift,
-                                                      uint32_t mask, uint32_t *__restrict__ hist, int ntiles) {
+                                                      uint32_t mask, uint32_t *__restrict__ hist, int ntiles,
+                                                      const int *run_if) {
+  if (run_if && *run_if == 0) return;
   __shared__ uint32_t h[RS_BINS];
   const int nbins = (int)mask + 1;
   for (int t = threadIdx.x; t < nbins; t += RS_THREADS) h[t] = 0;
@@ -52,7 +56,8 @@ __global__ void __launch_bounds__(RS_THREADS) rs_hist(const uint32_t *__restrict
 
 // One block per digit: exclusive scan of hist[d][0..ntiles) and its total.
 __global__ void __launch_bounds__(256) rs_rowscan(uint32_t *__restrict__ hist, int ntiles,
-                                                  uint32_t *__restrict__ totals) {
+                                                  uint32_t *__restrict__ totals, const int *run_if) {
+  if (run_if && *run_if == 0) return;
   __shared__ uint32_t wsum[8];
   __shared__ uint32_t carry;
   uint32_t *row = hist + (size_t)blockIdx.x * ntiles;
@@ -90,7 +95,8 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter(const uint32_t *__restr
                                                          uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                          int n, int shift, uint32_t mask,
                                                          const uint32_t *__restrict__ hist, int ntiles,
-                                                         const uint32_t *__restrict__ totals) {
+                                                         const uint32_t *__restrict__ totals, const int *run_if) {
+  if (run_if && *run_if == 0) return;
   __shared__ uint32_t wcount[RS_WARPS][RS_BINS];
   __shared__ uint32_t goff[RS_BINS];
   __shared__ uint32_t wtot[RS_WARPS];
@@ -176,7 +182,8 @@ size_t ds_radix_scratch_words(int n) {
 int ds_radix_passes(int key_bits) { return key_bits <= 0 ? 0 : (key_bits + RS_MAX_BITS - 1) / RS_MAX_BITS; }
 
 cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, int n,
-                          int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt) {
+                          int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt,
+                          const int *run_if) {
   *result_in_alt = false;
   if (n <= 0 || key_bits <= 0) return cudaSuccess;
   const int passes = ds_radix_passes(key_bits);
@@ -189,12 +196,13 @@ cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, ui
     const int shift = p * width;
     int bits = key_bits - shift < width ? key_bits - shift : width;
     const uint32_t mask = (1u << bits) - 1u;
-    cudaError_t e = ds_launch(rs_hist, dim3(ntiles), dim3(RS_THREADS), stream, ki, n, shift, mask, hist, ntiles);
+    cudaError_t e =
+        ds_launch(rs_hist, dim3(ntiles), dim3(RS_THREADS), stream, ki, n, shift, mask, hist, ntiles, run_if);
     if (e == cudaSuccess)
-      e = ds_launch(rs_rowscan, dim3((int)mask + 1), dim3(256), stream, hist, ntiles, totals);
+      e = ds_launch(rs_rowscan, dim3((int)mask + 1), dim3(256), stream, hist, ntiles, totals, run_if);
     if (e == cudaSuccess)
       e = ds_launch(rs_scatter, dim3(ntiles), dim3(RS_THREADS), stream, ki, vi, ko, vo, n, shift, mask, hist,
-                    ntiles, totals);
+                    ntiles, totals, run_if);
     if (e != cudaSuccess) return e;
     uint32_t *t = ki; ki = ko; ko = t;
     t = vi; vi = vo; vo = t;

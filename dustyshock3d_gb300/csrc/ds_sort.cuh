@@ -31,6 +31,8 @@ int ds_radix_passes(int key_bits);
 // pairs end in (keys, vals) or, when *result_in_alt, in (keys_alt, vals_alt).
 // Launch-only: capturable into a CUDA graph.  Returns the first failed
 // launch's status (cudaSuccess if every pass launched); the thread's
-// last-error state is left as the launches left it.
+// last-error state is left as the launches left it.  run_if: when given, the
+// kernels do nothing if *run_if == 0 at run time (the pairs stay as they were).
 cudaError_t ds_radix_sort(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, int n,
-                          int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt);
+                          int key_bits, uint32_t *scratch, cudaStream_t stream, bool *result_in_alt,
+                          const int *run_if = nullptr);

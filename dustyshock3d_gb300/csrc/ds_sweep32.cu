@@ -54,13 +54,52 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
   return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
+// After the density sum of particle i: the density (kernel normalisation in
+// FP64), the EOS, and the force sweep's FP32 inputs and CFL bound.
+template <bool HPP, int WHAT>
+__device__ __forceinline__ void density_epilogue(const SweepArgs &a, const TubeDesc &T, const Chunk &ch, int i,
+                                                 bool upd, bool zero, double rho, double hd, float hf,
+                                                 const Kahan &sum) {
+  if (upd) rho = rho + (((double)1 / (DS_PI_REF)) / (hd * hd * hd)) * sum.value();
+  if (zero || upd) a.st.rho[i] = rho;
+  if (WHAT == 0) {
+    double p = a.st.p[i];
+    if (upd) {
+      p = ds_eq_state(rho, a.st.e[i], T.type_of_state, T.gam, T.cs);
+      a.st.p[i] = p;
+    }
+    // force inputs and the CFL bound in FP32 (the force sweep is FP32)
+    const float rhof = (float)rho, pf = (float)p;
+    const float csf = sqrtf((float)T.gam * pf / rhof);
+    // .w: 1/h of the particle (frozen ones too: they are force partners)
+    const float hown = HPP ? a.pos32[i].w : (float)T.h;
+    a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
+    if (upd && (T.mode & M_CFL)) {
+      const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
+      const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
+      atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong((double)dt));
+    }
+  }
+}
+
+// The 4 warp flags of a chunk as one word (nbl_walk is 4-byte aligned per chunk).
+__device__ __forceinline__ uint32_t chunk_walk_flags(const SweepArgs &a, int c) {
+  return *reinterpret_cast<const uint32_t *>(a.nbl_walk + (size_t)c * (DS_SWEEP_THREADS / 32));
+}
+
 // LIST: the gas density sweep also records the force sweep's neighbours.  It
 // then walks the force sweep's stencil and screens with its cut-off
 // 2 max(h_i, h_j) (a superset of its own 2 h_i: the density adds only pairs
-// within 2 h_i, so its sum is unchanged), and writes each pair with r > 0 --
-// exactly the pairs the force sweep's own walk would accept, in its visiting
+// within 2 h_i, so its sum is unchanged), and writes every candidate that
+// passes (the particle itself too, which the force sweep's screen r > 0
+// drops) -- the pairs the force sweep's own walk would accept, in its visiting
 // order.  A warp with a particle beyond nbl_cap entries is flagged (one flag
 // per warp, no block barrier); the force sweep walks that warp's particles.
+// With list reuse (a.reuse) the recorded cut-off is 2 max(h_i, h_j) + skin,
+// and a tube that keeps its lists this step (TubeState::rebuild 0) neither
+// walks nor records here: k_density32_lst streams its lists, and only its
+// flagged warps walk (with its last re-sort's cells, which the skin covers),
+// recording nothing.
 #ifndef DS_DENS_LIST_MINB
 #define DS_DENS_LIST_MINB 6  // blocks per SM the list-recording density sweep is built for
 #endif
@@ -70,8 +109,11 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
   __shared__ float4 shtab[DS_NOFS32];
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
     const Chunk ch = a.chunks[c];
+    const bool record = !LIST || !a.reuse || a.tstate[ch.tube].rebuild;
+    if (LIST && !record && chunk_walk_flags(a, c) == 0u) continue;  // uniform per block: the lists serve it
+    const bool mine = record || a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)];
     const int i = ch.begin + threadIdx.x;
-    const bool valid = i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
+    const bool valid = mine && i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
     const TubeDesc &T = a.tubes[ch.tube];
     __syncthreads();  // the previous chunk's table is no longer read
     ds_fill_shift_table32(T, shtab);
@@ -90,6 +132,7 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
     const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
     const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
+    const float skin = LIST ? (float)T.skin : 0.0f;
     Stencil S{0, 0, 0, 0};
     const int own = upd ? (int)(a.skey[i] >> T.xl) : 0;  // own cell key
     if (upd) ds_stencil_from_key(T, own - T.key_base[s], a.st.x[i], a.st.y[i], a.st.z[i], S);
@@ -106,8 +149,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
           const float4 pj = a.pos32[j];
           const float r2 = r2_of(pj.x + ox, pj.y + oy, pj.z + oz);
           if (LIST) {
-            const float hc = HPP ? fmaxf(hf, pj.w) : hf;
-            return r2 < 4.0f * hc * hc;
+            const float rc = 2.0f * (HPP ? fmaxf(hf, pj.w) : hf) + skin;
+            return r2 < rc * rc;
           }
           return r2 < cut2;
         },
@@ -119,38 +162,90 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
             const float q = r2 > 0.0f ? r2 * rsqrtf(r2) * inv_h : 0.0f;
             sum.add(a.vm32[j].w * w_shape(q));
           }
-          if (LIST && r2 > 0.0f) {
+          if (LIST && record) {
             if (cnt < a.nbl_cap)
               nl[(size_t)cnt * DS_SWEEP_THREADS] = ((uint32_t)o5 << DS_OFS32_SHIFT) | (uint32_t)(j - sb);
             cnt++;
           }
         });
-    if (LIST) {
+    if (LIST && record) {
       const unsigned over = __ballot_sync(0xffffffffu, cnt > a.nbl_cap);
       if ((threadIdx.x & 31) == 0) a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)] = over != 0u;
       if (i < ch.end) a.nbl_cnt[i] = cnt;
     }
     if (!valid) continue;
-    if (upd) rho = rho + (((double)1 / (DS_PI_REF)) / (hd * hd * hd)) * sum.value();
-    if (zero || upd) a.st.rho[i] = rho;
-    if (WHAT == 0) {
-      double p = a.st.p[i];
-      if (upd) {
-        p = ds_eq_state(rho, a.st.e[i], T.type_of_state, T.gam, T.cs);
-        a.st.p[i] = p;
+    density_epilogue<HPP, WHAT>(a, T, ch, i, upd, zero, rho, hd, hf, sum);
+  }
+}
+
+// The gas density of a tube that keeps its lists this step: its recorded
+// entries (the particle itself among them) in the recording walk's order, each
+// added when within 2 h_i now -- the pairs and the order a walk of the same
+// cells would take, so the sum equals the walk's bit for bit; no walk, no
+// screen of candidates.  Warps flagged as overflowed are left to the walk
+// (k_density32), tubes that re-sort to the recording walk.
+#ifndef DS_DPIECE
+#define DS_DPIECE 4  // list entries per pipeline stage of the density stream
+#endif
+template <bool HPP>
+__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a) {
+  const unsigned FULL = 0xffffffffu;
+  __shared__ float4 shtab[DS_NOFS32];
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    const Chunk ch = a.chunks[c];
+    if (a.tstate[ch.tube].rebuild || chunk_walk_flags(a, c) == 0x01010101u) continue;  // uniform per block
+    const int i = ch.begin + threadIdx.x;
+    const TubeDesc &T = a.tubes[ch.tube];
+    __syncthreads();
+    ds_fill_shift_table32(T, shtab);
+    __syncthreads();
+    const bool listed = !a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)];
+    const bool valid = listed && i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
+    const bool upd = valid && a.st.ind[i] == 0;
+    double rho = valid ? a.st.rho[i] : 0.0;
+    if (upd) rho = 0.0;
+    const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
+    const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
+    const int sb = T.seg_begin[ch.species];
+    Kahan sum;
+    const int cnt = upd ? a.nbl_cnt[i] : 0;
+    const int cnt_w = __reduce_max_sync(FULL, cnt);
+    const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
+    uint32_t ent[DS_DPIECE];
+#pragma unroll
+    for (int t = 0; t < DS_DPIECE; t++) ent[t] = t < cnt ? __ldcs(nl + (size_t)t * DS_SWEEP_THREADS) : 0u;
+    for (int e = 0; e < cnt_w; e += DS_DPIECE) {
+      float4 pj[DS_DPIECE];
+      float mj[DS_DPIECE];
+#pragma unroll
+      for (int t = 0; t < DS_DPIECE; t++)
+        if (e + t < cnt) {
+          const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
+          pj[t] = a.pos32[j];
+          mj[t] = a.vm32[j].w;
+        }
+      uint32_t nxt[DS_DPIECE];
+#pragma unroll
+      for (int t = 0; t < DS_DPIECE; t++) {
+        const int q = e + DS_DPIECE + t;
+        nxt[t] = q < cnt ? __ldcs(nl + (size_t)q * DS_SWEEP_THREADS) : 0u;
       }
-      // force inputs and the CFL bound in FP32 (the force sweep is FP32)
-      const float rhof = (float)rho, pf = (float)p;
-      const float csf = sqrtf((float)T.gam * pf / rhof);
-      // .w: 1/h of the particle (frozen ones too: they are force partners)
-      const float hown = HPP ? a.pos32[i].w : (float)T.h;
-      a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
-      if (upd && (T.mode & M_CFL)) {
-        const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
-        const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
-        atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong((double)dt));
-      }
+#pragma unroll
+      for (int t = 0; t < DS_DPIECE; t++)
+        if (e + t < cnt) {
+          const float4 sh = shtab[ent[t] >> DS_OFS32_SHIFT];
+          const float r2 = r2_of(pj[t].x + (sh.x - pi.x), pj[t].y + (sh.y - pi.y), pj[t].z + (sh.z - pi.z));
+          if (r2 < cut2) {
+            const float q = r2 > 0.0f ? r2 * rsqrtf(r2) * inv_h : 0.0f;
+            sum.add(mj[t] * w_shape(q));
+          }
+        }
+#pragma unroll
+      for (int t = 0; t < DS_DPIECE; t++) ent[t] = nxt[t];
     }
+    if (!valid) continue;
+    density_epilogue<HPP, 0>(a, T, ch, i, upd, upd, rho, hd, hf, sum);
   }
 }
 
@@ -227,11 +322,6 @@ struct ForceSum {
   }
 };
 
-// The 4 warp flags of a chunk as one word (nbl_walk is 4-byte aligned per chunk).
-__device__ __forceinline__ uint32_t chunk_walk_flags(const SweepArgs &a, int c) {
-  return *reinterpret_cast<const uint32_t *>(a.nbl_walk + (size_t)c * (DS_SWEEP_THREADS / 32));
-}
-
 // Force sweep by walking the stencil.  With recorded lists it runs only the
 // warps flagged as overflowed.
 template <bool HPP, int CAP>
@@ -263,8 +353,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   }
 }
 
-// Force sweep over the recorded lists: no cell walk, no screening; entries in
-// the walk's order, so the sums equal the walk's.
+// Force sweep over the recorded lists: no cell walk; entries in the walk's
+// order, each tested against its exact cut-off, so the sums equal the walk's.
 #ifndef DS_FPIECE
 #define DS_FPIECE 2  // list entries per pipeline stage (measured: 2 beats 4)
 #endif
@@ -310,11 +400,40 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
       }
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++)
-        if (e + t < cnt) F.pair(shtab[ent[t] >> DS_OFS32_SHIFT], pj[t], vmj[t], hyj[t]);
+        if (e + t < cnt) {
+          // the recorded cut-off may exceed this step's (list reuse: by the
+          // skin), and the particle itself is listed; the screen keeps
+          // exactly the pairs the walk's screen would
+          const float4 sh = shtab[ent[t] >> DS_OFS32_SHIFT];
+          if (F.screen(pj[t], sh.x - F.pi.x, sh.y - F.pi.y, sh.z - F.pi.z)) F.pair(sh, pj[t], vmj[t], hyj[t]);
+        }
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++) ent[t] = nxt[t];
     }
     if (act) F.store(a, i);
+  }
+}
+
+// Parity hook: the recorded force lists of one tube's gas, by caller index.
+// count[i]: entries recorded for particle i, or -1 when its warp walks (an
+// entry beyond the lists' capacity); nbr[i * cap + k]: the caller index of its
+// k-th entry (k < min(count[i], cap)).
+__global__ void k_debug_force_lists(SweepArgs a, int tube, int cap, int *count, int *nbr) {
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    const Chunk ch = a.chunks[c];
+    const int q = ch.begin + threadIdx.x;
+    if (ch.tube != tube || q >= ch.end) continue;
+    const int pi = a.st.pid[q];
+    if (a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)]) {
+      count[pi] = -1;
+      continue;
+    }
+    const int n = a.nbl_cnt[q];
+    count[pi] = n;
+    const int sb = a.tubes[ch.tube].seg_begin[ch.species];
+    const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
+    for (int e = 0; e < n && e < cap && e < a.nbl_cap; e++)
+      nbr[(size_t)pi * cap + e] = a.st.pid[sb + (int)(nl[(size_t)e * DS_SWEEP_THREADS] & DS_SLOT32_MASK)];
   }
 }
 
@@ -339,6 +458,17 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
   if (!a.nchunks) return;
   if (depth >= 64) launch_density32<64>(a, hpp, what, s);
   else launch_density32<32>(a, hpp, what, s);
+}
+
+void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s) {
+  if (!a.nchunks || !a.nbl || !a.reuse) return;
+  if (hpp) k_density32_lst<true><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  else k_density32_lst<false><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+}
+
+void ds_launch_debug_force_lists(const SweepArgs &a, int tube, int cap, int *count, int *nbr, cudaStream_t s) {
+  if (!a.nchunks || !a.nbl) return;
+  k_debug_force_lists<<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a, tube, cap, count, nbr);
 }
 
 // With recorded lists: the list kernel, then the walk over overflowed chunks.

@@ -96,6 +96,7 @@ class Params:
     stencil: int = 1      # cells searched on each side: 1 (the reference's 27 cells) or 2 (125 cells)
     list_depth: int = 0   # FP32 sweeps: candidate-list entries per thread (0 -> 32; 64)
     force_list: int = 0   # FP32: recorded force neighbours per gas particle (0 -> 256; -1 -> off)
+    list_skin: float = 0.0  # FP32 with force lists: reuse the lists across steps, skin in units of h (0 -> off)
     precision: str = "fp64"  # "fp64" or "fp32" (FP32 neighbour sums, FP64 state/IDIC)
     mode: Mode = field(default_factory=Mode)
 
@@ -125,7 +126,7 @@ _INIT_ORDER = [
 
 # extension names that take one number (the Init.txt fields may be set by name too)
 _FLOAT_FIELDS = {name for name, _ in _INIT_ORDER} | {"Gam_g", "Speed_of_sound_gas", "t_empty", "cell_w", "idic_w",
-                                                      "cfl"}
+                                                      "cfl", "list_skin"}
 
 
 def _leading_number(line: str, kind):
@@ -187,7 +188,7 @@ def write_init_txt(P: Params, extensions: bool = True) -> str:
         v = getattr(P, name)
         out.append(f"{v!r}\t\t// {name}" if kind is float else f"{int(v)}\t\t// {name}")
     if extensions:
-        for k in ("Gam_g", "Speed_of_sound_gas", "t_empty", "cell_w", "idic_w", "cfl"):
+        for k in ("Gam_g", "Speed_of_sound_gas", "t_empty", "cell_w", "idic_w", "cfl", "list_skin"):
             out.append(f"{k} = {getattr(P, k)!r}")
         out.append(f"n_dust = {P.n_dust}")
         out.append(f"stencil = {P.stencil}")

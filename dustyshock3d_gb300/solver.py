@@ -257,6 +257,24 @@ class Solver:
         reference's output-only sweep, kernel.cu:2029-2043), on demand."""
         _lib.check(self.L, self.ctx, self.L.ds_dust_density(self.ctx), "ds_dust_density")
 
+    def list_stats(self, tube: int = 0):
+        """(steps that re-sorted and recorded the neighbour lists, steps taken)."""
+        r, n = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        _lib.check(self.L, self.ctx, self.L.ds_list_stats(self.ctx, tube, ctypes.byref(r), ctypes.byref(n)),
+                   "ds_list_stats")
+        return int(r.value), int(n.value)
+
+    def debug_force_lists(self, tube: int = 0, cap: int = 512):
+        """The recorded force lists of the tube's gas by caller index: (count,
+        nbr) with count[i] = entries of particle i (-1: its warp walks) and
+        nbr[i, :count[i]] their caller indices."""
+        n = self.n[tube][0]
+        count = np.zeros(max(n, 1), dtype=np.int32)
+        nbr = np.full((max(n, 1), cap), -1, dtype=np.int32)
+        _lib.check(self.L, self.ctx, self.L.ds_debug_force_lists(self.ctx, tube, cap, _ip(count), _ip(nbr)),
+                   "ds_debug_force_lists")
+        return count[:n], nbr[:n]
+
     def kernels_per_step(self):
         k = ctypes.c_int(0)
         _lib.check(self.L, self.ctx, self.L.ds_kernels_per_step(self.ctx, ctypes.byref(k)), "ds_kernels_per_step")

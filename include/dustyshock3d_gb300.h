@@ -121,6 +121,25 @@ typedef struct ds_params {
   double R_dust[DS_MAX_DUST];       /* R_dust_k for t_stop = R/(c_s rho) (IDIC.h:86) */
   double t_stop_const[DS_MAX_DUST]; /* DS_MODE_TSTOP_CONST                        */
   double eps_empty[DS_MAX_DUST];    /* eps of a cell failing its guard (kernel.cu:2200, 2209) */
+  double list_skin;          /* FP32 path with force lists: reuse of the recorded neighbour
+                                lists across steps (0 -> off: every step sorts, walks and
+                                records).  The density sweep records the pairs within
+                                2 max(h_i, h_j) + list_skin x h; later steps stream those
+                                lists (density and force, each pair tested against its exact
+                                cut-off) and skip the sort and the cell walk, until the
+                                tube's particles have moved far enough, relative to each
+                                other, that a pair outside the lists could be within its
+                                cut-off.  That test runs on the device at the start of every
+                                step, per tube, from the displacements since the lists were
+                                recorded: per neighbour cell their mean and largest deviation
+                                from it; a tube re-sorts when, for two cells within one cell
+                                beyond the recording walk's reach, the two deviations plus
+                                the difference of the means reach the skin, or when twice
+                                the largest deviation plus the spread of all cell means
+                                reaches the skin plus a cell width.  Neighbour cells are
+                                widened so that the recorded cut-off stays within the
+                                stencil.  Ignored (off) on the FP64 path, without force
+                                lists, and with DS_MODE_DUST_RHO. */
 } ds_params;
 
 typedef struct ds_ctx ds_ctx;
@@ -372,6 +391,20 @@ ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms)
 
 /* Number of kernels one step launches (the library's own kernels). */
 ds_status ds_kernels_per_step(ds_ctx *c, int *count);
+
+/* List reuse (ds_params.list_skin): steps of the tube that re-sorted and
+ * recorded its neighbour lists, and steps taken.  No counterpart in the
+ * reference, which rebuilds its lists every step (kernel.cu:1937-1995). */
+ds_status ds_list_stats(ds_ctx *c, int tube, long long *rebuilds, long long *steps);
+
+/* Parity hook (FP32 path with force lists): the neighbour lists the density
+ * sweep last recorded for the tube's gas, by caller index.  count[i] = the
+ * entries of particle i (-1: its warp walks the cells instead, an entry beyond
+ * the lists' capacity), nbr[i * cap + k] = the caller index of its k-th entry,
+ * k < min(count[i], cap).  Tests use it to check that reused lists still hold
+ * every pair within the cut-off.  No counterpart in the reference, whose
+ * linked cell lists (kernel.cu:1937-1995) are walked afresh every step. */
+ds_status ds_debug_force_lists(ds_ctx *c, int tube, int cap, int *count, int *nbr);
 
 /* Device bytes held by the context, and particles per tube. */
 ds_status ds_memory_bytes(ds_ctx *c, long long *bytes);

@@ -1,0 +1,198 @@
+"""Reuse of the recorded neighbour lists across steps (FP32 path, list_skin > 0).
+
+The density sweep records, per gas particle, every partner within
+2 max(h_i, h_j) + skin; while a tube's particles have not moved far enough
+relative to each other, later steps stream those lists instead of sorting and
+walking the cells.  Checked here:
+  * coverage: at every step that kept its lists, the lists held every pair
+    within its cut-off at that step's positions (scipy KD-tree on the host);
+  * the results track the FP64 oracle as the FP32 path does without reuse;
+  * streamed lists and walked cells give the same sums bit for bit (the
+    recorded order is the walk's), and a tube's arithmetic does not depend on
+    the other tubes of its batch;
+  * replacing a tube's state makes the next step re-sort.
+(The reference rebuilds its lists every step, kernel.cu:1937-1995.)
+"""
+import numpy as np
+import pytest
+
+from dustyshock3d_gb300 import ic
+from dustyshock3d_gb300.solver import Solver
+from oracle.oracle import OracleState
+
+pytestmark = pytest.mark.gpu
+
+MOVED = ("x", "y", "z", "vx", "vy", "vz", "rho")
+
+
+def small_tube(**kw):
+    args = dict(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25))
+    args.update(kw)
+    P, sp = ic.dusty_sod_tube(**args)
+    P.precision = "fp32"
+    return P, sp
+
+
+def pairs_within_cutoff(g, P, slack=1e-5):
+    """Every ordered pair (i, j), i free, with 0 < r < 2 max(h_i, h_j) (1 - slack)
+    (periodic y and z to the nearest image): the pairs the force sweep needs.
+    The slack leaves out pairs whose FP32 distance may round across the cut-off."""
+    from scipy.spatial import cKDTree
+    Ly, Lz = P.Y_max - P.Y_min, P.Z_max - P.Z_min
+    x0 = g.x.min()
+    bx = 3.0 * (g.x.max() - x0) + 1.0
+    pts = np.stack([g.x - x0, np.mod(g.y - P.Y_min, Ly), np.mod(g.z - P.Z_min, Lz)], 1)
+    pts[:, 1] = np.where(pts[:, 1] >= Ly, 0.0, pts[:, 1])
+    pts[:, 2] = np.where(pts[:, 2] >= Lz, 0.0, pts[:, 2])
+    pr = cKDTree(pts, boxsize=[bx, Ly, Lz]).query_pairs(2.0 * g.h.max(), output_type="ndarray")
+    i, j = pr[:, 0], pr[:, 1]
+    dx = g.x[i] - g.x[j]
+    dy = g.y[i] - g.y[j]
+    dy -= Ly * np.round(dy / Ly)
+    dz = g.z[i] - g.z[j]
+    dz -= Lz * np.round(dz / Lz)
+    r = np.sqrt(dx * dx + dy * dy + dz * dz)
+    keep = (r > 0) & (r < 2.0 * np.maximum(g.h[i], g.h[j]) * (1.0 - slack))
+    i, j = i[keep], j[keep]
+    i, j = np.concatenate([i, j]), np.concatenate([j, i])
+    free = g.ind[i] == 0
+    return i[free], j[free]
+
+
+def assert_lists_cover(count, nbr, i, j, what):
+    """Every required pair (i, j) appears in i's recorded list (particles whose
+    warp walks the cells are exempt)."""
+    n = len(count)
+    assert (count <= nbr.shape[1]).all(), "export capacity too small"
+    walked = count[i] < 0
+    i, j = i[~walked], j[~walked]
+    c = np.maximum(count, 0)
+    rows = np.repeat(np.arange(n, dtype=np.int64), c)
+    cols = nbr[np.arange(nbr.shape[1])[None, :] < c[:, None]].astype(np.int64)
+    listed = np.unique(rows * n + cols)
+    need = i.astype(np.int64) * n + j
+    missing = ~np.isin(need, listed)
+    assert not missing.any(), f"{what}: {missing.sum()} of {len(need)} pairs within the cut-off are not listed"
+
+
+@pytest.mark.parametrize("skin,cap", [(0.1, 0), (0.25, 0), (0.6, 0), (0.25, 100)])
+def test_kept_lists_hold_every_pair_within_the_cutoff(skin, cap):
+    """Step by step: whenever a step kept its lists, they held every pair within
+    2 max(h_i, h_j) at the positions that step used (those before it)."""
+    P, sp = small_tube()
+    P.list_skin = skin
+    P.force_list = cap
+    kept = 0
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(1)
+        rb_prev, _ = S.list_stats(0)
+        for _ in range(24):
+            before = S.get_species(0, 0)
+            S.step(1)
+            rb, ns = S.list_stats(0)
+            if rb == rb_prev:
+                kept += 1
+                count, nbr = S.debug_force_lists(0, cap=512)
+                i, j = pairs_within_cutoff(before, P)
+                assert_lists_cover(count, nbr, i, j, f"skin {skin}, step {ns}")
+            rb_prev = rb
+        assert ns == 25
+    assert kept >= 3, f"skin {skin}: only {kept} of 24 steps kept their lists"
+    assert kept < 24 or skin >= 0.6
+
+
+@pytest.mark.parametrize("skin", [0.1, 0.3])
+def test_reuse_tracks_the_oracle(skin):
+    """FP32 with reused lists vs the FP64 oracle after 16 steps: the FP32 path's
+    own bounds (relative L1 of gas density <= 1e-5, mean velocity error <=
+    1e-4 of the velocity scale), and within 1e-5 (max, relative) of the FP32
+    path without reuse."""
+    P, sp = small_tube()
+    P0 = P.copy()
+    P.list_skin = skin
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(16)
+        g, d = S.get_species(0, 0), S.get_species(0, 1)
+        rb, ns = S.list_stats(0)
+    assert ns == 16 and rb < ns
+    with Solver(P0) as S:
+        S.set_tube(0, sp)
+        S.step(16)
+        g0 = S.get_species(0, 0)
+    P64 = P0.copy()
+    P64.precision = "fp64"
+    O = OracleState(P64, sp).step(16)
+    o = O.species[0]
+    l1 = np.abs(g.rho - o.rho).sum() / np.abs(o.rho).sum()
+    assert l1 < 1e-5, l1
+    vscale = np.abs(o.vx).max()
+    assert np.abs(g.vx - o.vx).mean() / vscale < 1e-4
+    assert np.abs(d.vx - O.species[1].vx).mean() / vscale < 1e-4
+    rel = np.abs(g.rho - g0.rho) / np.abs(g0.rho)
+    assert rel.max() < 1e-5, rel.max()
+
+
+def test_streamed_lists_equal_walked_cells():
+    """With reuse, warps that stream their lists and warps that walk the
+    recorded cells (lists of 100 entries: most overflow) give the same results
+    as lists that never overflow, bit for bit, over steps that keep and steps
+    that rebuild."""
+    P, sp = small_tube()
+    P.list_skin = 0.3
+    out = []
+    for cap in (0, 100):
+        Q = P.copy()
+        Q.force_list = cap
+        with Solver(Q) as S:
+            S.set_tube(0, sp)
+            S.step(12)
+            out.append([S.get_species(0, s) for s in range(2)])
+            rb, ns = S.list_stats(0)
+        assert rb < ns
+    for s in range(2):
+        for f in MOVED:
+            a, b = getattr(out[0][s], f), getattr(out[1][s], f)
+            assert np.array_equal(a, b), f"species {s} {f}"
+
+
+def test_batched_tubes_with_and_without_reuse_equal_alone():
+    """Each tube decides on its own: a batch of tubes with different skins (one
+    without reuse) gives every tube the results it gets alone, bit for bit."""
+    cases = [small_tube(), small_tube(eps=0.1, t_s=1e-2, rho_R=0.25, p_R=0.2),
+             small_tube(dx_left=1 / 48, Ly=0.375, eps=3.0, t_s=3e-4)]
+    for (P, _), skin in zip(cases, (0.25, 0.0, 0.5)):
+        P.list_skin = skin
+    with Solver([c[0] for c in cases]) as S:
+        for t, (P, sp) in enumerate(cases):
+            S.set_tube(t, sp)
+        S.step(10)
+        batched = [[S.get_species(t, s) for s in range(2)] for t in range(len(cases))]
+        stats = [S.list_stats(t) for t in range(len(cases))]
+    assert stats[1] == (10, 10) and stats[0][0] < 10 and stats[2][0] < 10
+    for t, (P, sp) in enumerate(cases):
+        with Solver(P) as S:
+            S.set_tube(0, sp)
+            S.step(10)
+            alone = [S.get_species(0, s) for s in range(2)]
+            assert S.list_stats(0) == stats[t]
+        for s in range(2):
+            for f in MOVED:
+                assert np.array_equal(getattr(batched[t][s], f), getattr(alone[s], f)), f"tube {t} species {s} {f}"
+
+
+def test_replacing_the_state_makes_the_next_step_resort():
+    P, sp = small_tube()
+    P.list_skin = 0.6
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(3)
+        rb0, _ = S.list_stats(0)
+        S.step(1)
+        rb1, _ = S.list_stats(0)
+        assert rb1 == rb0, "a large skin should keep the lists for the fourth step"
+        S.set_tube(0, [S.get_species(0, s) for s in range(2)])
+        S.step(1)
+        rb2, ns = S.list_stats(0)
+        assert rb2 == rb1 + 1 and ns == 5
