@@ -217,12 +217,12 @@ void build_desc(const ds_params &P, TubeDesc &T) {
   T.ox = P.X_min; T.oy = P.Y_min; T.oz = P.Z_min;
   const bool proper = (P.mode & DS_MODE_GRID_PROPER) != 0;
   // list reuse (FP32 path with force lists): record 2 max(h_i, h_j) + skin and
-  // widen the cells so that the stencil's cells still cover that cut-off
+  // widen the cells by the skin, so that every cell's walk keeps its radius
+  // (a cut-off c within r cells of width w: c + skin within r cells of w + skin)
   const bool reuse = P.list_skin > 0 && P.precision == DS_PRECISION_FP32 && P.force_list != -1 && proper &&
                      !(P.mode & DS_MODE_DUST_RHO);
   T.skin = reuse ? P.list_skin * P.h : 0.0;
-  const int nst = proper && P.stencil > 1 ? P.stencil : 1;
-  const double w = (P.cell_w > 0 ? P.cell_w : 2.0 * P.h) + T.skin / nst;
+  const double w = (P.cell_w > 0 ? P.cell_w : 2.0 * P.h) + T.skin;
   T.Cnx = (int)((P.X_max - P.X_min) / w);
   T.Cny = (int)((P.Y_max - P.Y_min) / w);
   T.Cnz = (int)((P.Z_max - P.Z_min) / w);
@@ -695,7 +695,12 @@ ds_status finalize(ds_ctx *c) {
   DA(c->stage, (size_t)NF * N + (N + 1) / 2 + 1);  // download staging: every field, then Ind
   if (c->any_fp32 && c->params[0].force_list != -1 && !c->ch_gas.empty()) {
     // the force sweep's neighbours, recorded by the gas density sweep
-    c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : 256;
+    // default capacity: 256 entries (interior gas has ~80 partners within
+    // 2 max(h_i, h_j), shocked gas more); 512 when lists are recorded with a
+    // skin, whose shell adds partners
+    bool skin = false;
+    for (const auto &T : c->tdesc) skin = skin || T.skin > 0.0;
+    c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : (skin ? 512 : 256);
     DA(c->nbl, c->ch_gas.size() * (size_t)c->nbl_cap * DS_CHUNK);
     DA(c->nbl_cnt, N);
     DA(c->nbl_walk, c->ch_gas.size() * (DS_SWEEP_THREADS / 32));

@@ -114,9 +114,10 @@ typedef struct ds_params {
                                 (0 -> 32); an autotuner choice                         */
   int force_list;            /* FP32 path: neighbour entries per gas particle that the
                                 density sweep records for the force sweep, which then
-                                reads them instead of walking the cells again (0 -> 256;
-                                -1 -> off); a 128-particle chunk holding a particle with
-                                more neighbours walks.  Results are the same either way. */
+                                reads them instead of walking the cells again (0 -> 256,
+                                or 512 with a list_skin; -1 -> off); a warp holding a
+                                particle with more neighbours walks.  Results are the same
+                                either way. */
   double mass_ratio[DS_MAX_DUST];   /* mas_gas_dust_k (kernel.cu:1499-1502)       */
   double R_dust[DS_MAX_DUST];       /* R_dust_k for t_stop = R/(c_s rho) (IDIC.h:86) */
   double t_stop_const[DS_MAX_DUST]; /* DS_MODE_TSTOP_CONST                        */

@@ -369,7 +369,14 @@ void orc_idic_solve_cell(int n, const double *eps, const double *t, double vg, c
 /* One step, kernel.cu:1929-2523                                              */
 /* ------------------------------------------------------------------------ */
 
-int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken) {
+/* The step in two parts, as the reference runs it (kernel.cu:1937-2566): the
+ * lists, the gas density and the EOS (and the dust density), ending with the
+ * CFL candidate min h/(c_s + |v|) over the updated gas (+inf without CFL);
+ * then t_stop, the step size, the IDIC averages, the force, the implicit
+ * solve and the update.  The split lets a slab decomposition set the ghosts'
+ * density and pressure and the global CFL minimum between the parts; orc_step
+ * runs both. */
+int orc_step_density(const orc_params *P, orc_species *sp, double *dtmin_out) {
   orc_grid G;
   orc_grid_setup(P, &G);
   {
@@ -432,6 +439,42 @@ int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken)
       free(upd);
     }
 
+  /* CFL candidate (extension): the smallest h / (c_s + |v|) over the updated gas */
+  double dtmin = INFINITY;
+  if (P->flags & ORC_CFL)
+    for (int i = 0; i < Ng; i++) {
+      if (gas->ind[i] != 0) continue;
+      double c = sqrt(Gam_g * gas->p[i] / gas->rho[i]);
+      double v = sqrt(gas->vx[i] * gas->vx[i] + gas->vy[i] * gas->vy[i] + gas->vz[i] * gas->vz[i]);
+      double hi = hpp ? gas->h[i] : P->h;
+      double dt = hi / (c + v);
+      if (dt < dtmin) dtmin = dt;
+    }
+  if (dtmin_out) *dtmin_out = dtmin;
+  for (int s = 0; s < ns; s++) { free(head[s]); free(next[s]); }
+  return status;
+}
+
+int orc_step_complete(const orc_params *P, orc_species *sp, double *Tm, double dtmin, double *dt_taken) {
+  orc_grid G;
+  orc_grid_setup(P, &G);
+  const int nd = P->n_dust, ns = 1 + nd;
+  orc_species *gas = &sp[0];
+  const int Ng = gas->n;
+  const double Gam_g = P->Gam_g;
+  int status = 0;
+  /* the lists again: the positions have not changed since the density part */
+  int *head[1 + ORC_MAX_DUST], *next[1 + ORC_MAX_DUST];
+  {
+    int *tail = (int *)malloc(sizeof(int) * (G.ncells + 1));
+    for (int s = 0; s < ns; s++) {
+      head[s] = (int *)malloc(sizeof(int) * (G.ncells + 1));
+      next[s] = (int *)malloc(sizeof(int) * (sp[s].n > 0 ? sp[s].n : 1));
+      orc_list(&G, &sp[s], head[s], next[s], tail);
+    }
+    free(tail);
+  }
+
   /* stopping time (IDIC.h:78-91, kernel.cu:2049-2053): gas p, rho at the
    * dust particle's index (reference quirk) */
   if (!(P->flags & ORC_TSTOP_CONST)) {
@@ -448,15 +491,6 @@ int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken)
   /* step size: fixed tau (kernel.cu:1931) or CFL (extension) */
   double tau = P->tau;
   if (P->flags & ORC_CFL) {
-    double dtmin = INFINITY;
-    for (int i = 0; i < Ng; i++) {
-      if (gas->ind[i] != 0) continue;
-      double c = sqrt(Gam_g * gas->p[i] / gas->rho[i]);
-      double v = sqrt(gas->vx[i] * gas->vx[i] + gas->vy[i] * gas->vy[i] + gas->vz[i] * gas->vz[i]);
-      double hi = hpp ? gas->h[i] : P->h;
-      double dt = hi / (c + v);
-      if (dt < dtmin) dtmin = dt;
-    }
     tau = P->cfl * dtmin;
     if (*Tm + tau > P->T_end) tau = P->T_end - *Tm;
   }
@@ -626,6 +660,13 @@ int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken)
   free(psx); free(psy); free(psz);
   for (int s = 0; s < ns; s++) { free(head[s]); free(next[s]); free(ckey[s]); }
   return status;
+}
+
+int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken) {
+  double dtmin = INFINITY;
+  int status = orc_step_density(P, sp, &dtmin);
+  if (status < 0) return status;
+  return status | orc_step_complete(P, sp, Tm, dtmin, dt_taken);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -75,6 +75,13 @@ typedef struct orc_species {
  * of the library's DS_FLAG_* bits that the step raised: 1 IDIC index out of
  * range, 8 a cut-off 2h past the stencil's cells on the proper grid. */
 int orc_step(const orc_params *P, orc_species *sp, double *Tm, double *dt_taken);
+/* orc_step in two parts (what orc_step runs): the lists, densities and EOS,
+ * with the CFL candidate min h / (c_s + |v|) over the updated gas (+inf
+ * without CFL); then the rest of the step with the step size taken from
+ * dtmin (CFL) or tau.  Between them a caller may overwrite the density and
+ * pressure of frozen particles (slab ghosts) and dtmin (a global minimum). */
+int orc_step_density(const orc_params *P, orc_species *sp, double *dtmin);
+int orc_step_complete(const orc_params *P, orc_species *sp, double *Tm, double dtmin, double *dt_taken);
 
 /* Linked lists of one species exactly as the reference builds them
  * (kernel.cu:1937-1955): head[ncells+1], next[n].  Returns ncells. */

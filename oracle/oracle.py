@@ -89,6 +89,13 @@ def lib():
             L.orc_step.argtypes = [ctypes.POINTER(OrcParams), ctypes.POINTER(OrcSpecies),
                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.orc_step.restype = ctypes.c_int
+            L.orc_step_density.argtypes = [ctypes.POINTER(OrcParams), ctypes.POINTER(OrcSpecies),
+                                           ctypes.POINTER(ctypes.c_double)]
+            L.orc_step_density.restype = ctypes.c_int
+            L.orc_step_complete.argtypes = [ctypes.POINTER(OrcParams), ctypes.POINTER(OrcSpecies),
+                                            ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_double)]
+            L.orc_step_complete.restype = ctypes.c_int
             L.orc_build_list.argtypes = [ctypes.POINTER(OrcParams), ctypes.POINTER(OrcSpecies), _IP, _IP]
             L.orc_build_list.restype = ctypes.c_int
             for name in ("orc_cell_keys", "orc_idic_keys"):
