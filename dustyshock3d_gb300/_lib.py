@@ -96,6 +96,13 @@ SIGNATURES = {
     "ds_list_stats": ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
                       ctypes.c_int),
     "ds_debug_force_lists": ([_VP, ctypes.c_int, ctypes.c_int, _IP, _IP], ctypes.c_int),
+    "ds_step_density": ([_VP], ctypes.c_int),
+    "ds_get_cfl_min": ([_VP, ctypes.c_int, _DP], ctypes.c_int),
+    "ds_set_cfl_min": ([_VP, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+    "ds_set_gas_hydro": ([_VP, ctypes.c_int, ctypes.c_int, _IP, _DP, _DP], ctypes.c_int),
+    "ds_step_complete": ([_VP], ctypes.c_int),
+    "ds_set_time": ([_VP, ctypes.c_int, ctypes.c_double, ctypes.c_longlong], ctypes.c_int),
+    "ds_idic_columns": ([ctypes.POINTER(DsParams), ctypes.c_int, _DP, _IP], ctypes.c_int),
     "ds_cell_lists_noalloc": ([ctypes.POINTER(DsParams), ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                                _VP, _VP], ctypes.c_int),
     "ds_host_alloc": ([ctypes.POINTER(_VP), ctypes.c_longlong], ctypes.c_int),

@@ -108,6 +108,13 @@ struct ds_ctx {
   // start-of-step test (force: every tube re-sorts; any: some tube re-sorts)
   bool reuse = false;
   float4 *pos_ref = nullptr, *disp = nullptr, *cellstat = nullptr;
+  // split step (ds_step_density .. ds_step_complete): 1 between the parts;
+  // ialt: the IDIC key sort's result is in the alternate buffers
+  int split = 0;
+  bool ialt = false;
+  int *hy_idx = nullptr;       // ds_set_gas_hydro: caller indices, rho, p on the device
+  double *hy_val = nullptr;
+  int hy_cap = 0;
   int *d_force = nullptr, *d_any = nullptr;
   uint32_t *kin = nullptr, *vin = nullptr, *kalt = nullptr, *valt = nullptr;
   uint32_t *ikin = nullptr, *ivin = nullptr, *ikalt = nullptr, *ivalt = nullptr;
@@ -372,6 +379,19 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   return a;
 }
 
+// The gas sweeps' arguments, with the recorded force lists when there are any.
+SweepArgs gas_sweep_args(ds_ctx *c) {
+  SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
+  if (c->nbl) {
+    ag.nbl = c->nbl;
+    ag.nbl_cnt = c->nbl_cnt;
+    ag.nbl_walk = c->nbl_walk;
+    ag.nbl_cap = c->nbl_cap;
+    ag.reuse = c->reuse ? 1 : 0;
+  }
+  return ag;
+}
+
 // The sorted keys' buffer of the FP32 path's sorts (a fixed number of passes).
 const uint32_t *fast_skey(const ds_ctx *c) {
   return (ds_radix_passes(c->key_bits + c->xl) & 1) ? c->kalt : c->kin;
@@ -412,23 +432,18 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorde
   c->parity ^= 1;
 }
 
-// The step after the sort: sweeps, IDIC, update.  ev: optional phase events.
-void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullptr,
-                     cudaEvent_t after_force = nullptr) {
+// The step after the sort, first part: the IDIC key sort and the densities
+// (with the EOS and the force sweep's per-particle inputs).  ev: optional
+// phase events.
+void enqueue_density(ds_ctx *c, cudaEvent_t *ev) {
   cudaStream_t s = c->stream;
   bool alt = false;
   ds_radix_sort(c->ikin, c->ivin, c->ikalt, c->ivalt, c->N, c->ikey_bits, c->rs_scratch, s, &alt);
+  c->ialt = alt;
   if (ev) cudaEventRecord(ev[1], s);
   const bool fp32 = c->any_fp32;
-  SweepArgs ag = sweep_args(c, c->d_ch_gas, (int)c->ch_gas.size());
+  SweepArgs ag = gas_sweep_args(c);
   SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
-  if (c->nbl) {
-    ag.nbl = c->nbl;
-    ag.nbl_cnt = c->nbl_cnt;
-    ag.nbl_walk = c->nbl_walk;
-    ag.nbl_cap = c->nbl_cap;
-    ag.reuse = c->reuse ? 1 : 0;
-  }
   const int depth = c->params[0].list_depth;
   if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
@@ -438,6 +453,16 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
   }
   if (ev) cudaEventRecord(ev[2], s);
+}
+
+// The rest of the step: t_stop, the step size, the force, the IDIC cell sums
+// and solve, the update and the clock.
+void enqueue_rest(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullptr,
+                  cudaEvent_t after_force = nullptr) {
+  cudaStream_t s = c->stream;
+  const bool fp32 = c->any_fp32;
+  SweepArgs ag = gas_sweep_args(c);
+  const int depth = c->params[0].list_depth;
   if (after_density) cudaEventRecord(after_density, s);
   if (fp32 && c->wstream) {  // the overflow walk beside t_stop, dt and the list kernel
     cudaEventRecord(c->e_wfork, s);
@@ -458,8 +483,8 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
   }
   if (ev) cudaEventRecord(ev[3], s);
   if (after_force) cudaEventRecord(after_force, s);
-  const uint32_t *ik = alt ? c->ikalt : c->ikin;
-  const uint32_t *iv = alt ? c->ivalt : c->ivin;
+  const uint32_t *ik = c->ialt ? c->ikalt : c->ikin;
+  const uint32_t *iv = c->ialt ? c->ivalt : c->ivin;
   ds_launch_idic_reduce(ik, iv, c->N, c->nikeys, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st,
                         c->ca, fp32, s);
   ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, fp32, s);
@@ -468,8 +493,16 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
   ds_launch_step_end(c->d_tstate, c->ntubes, s);
 }
 
-void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
-  if (ev) cudaEventRecord(ev[0], c->stream);
+// The step after the sort: sweeps, IDIC, update.  ev: optional phase events.
+void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullptr,
+                     cudaEvent_t after_force = nullptr) {
+  enqueue_density(c, ev);
+  enqueue_rest(c, ev, after_density, after_force);
+}
+
+// The start of a step: the clocks and, with list reuse, which tubes keep
+// their lists; then the sort.
+void enqueue_step_begin(ds_ctx *c) {
   ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->stream);
   if (c->reuse)  // which tubes keep their lists this step
     ds_launch_list_test(c->d_tubes, c->d_tstate, c->ntubes, c->d_ch_gas, (int)c->ch_gas.size(),
@@ -477,6 +510,11 @@ void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
                         c->d_nseg_species, c->nnseg, c->nkeys, c->cell_start, c->xl, c->krad, c->cellstat,
                         c->d_force, c->d_any, c->stream);
   enqueue_sort(c, false, nullptr, true);
+}
+
+void enqueue_step(ds_ctx *c, cudaEvent_t *ev) {
+  if (ev) cudaEventRecord(ev[0], c->stream);
+  enqueue_step_begin(c);
   enqueue_physics(c, ev);
   if (ev) cudaEventRecord(ev[4], c->stream);
 }
@@ -1455,6 +1493,124 @@ ds_status ds_list_stats(ds_ctx *c, int tube, long long *rebuilds, long long *ste
   CK(cudaStreamSynchronize(c->stream));
   if (rebuilds) *rebuilds = c->reuse ? ts.nrebuild : ts.nstep;  // without reuse every step re-sorts
   if (steps) *steps = ts.nstep;
+  return DS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Split step (slab decomposition of one tube across processes)
+// ---------------------------------------------------------------------------
+
+ds_status ds_step_density(ds_ctx *c) {
+  if (!c) return DS_ERR_ARG;
+  ds_status st = finalize(c);
+  if (st != DS_OK) return st;
+  if (c->split) return fail(c, DS_ERR_STATE, "ds_step_density: the previous step is not complete (ds_step_complete)");
+  CK(cudaSetDevice(c->device));
+  enqueue_step_begin(c);
+  enqueue_density(c, nullptr);
+  CK(cudaGetLastError());
+  c->split = 1;
+  CK(cudaStreamSynchronize(c->stream));
+  return check_flags(c);
+}
+
+ds_status ds_get_cfl_min(ds_ctx *c, int tube, double *dtmin) {
+  if (!c || tube < 0 || tube >= c->ntubes || !dtmin) return DS_ERR_ARG;
+  if (!c->split) return fail(c, DS_ERR_STATE, "ds_get_cfl_min: between ds_step_density and ds_step_complete only");
+  CK(cudaSetDevice(c->device));
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, &c->d_tstate[tube].dtmin_bits, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  memcpy(dtmin, &bits, sizeof(double));
+  return DS_OK;
+}
+
+ds_status ds_set_cfl_min(ds_ctx *c, int tube, double dtmin) {
+  if (!c || tube < 0 || tube >= c->ntubes) return DS_ERR_ARG;
+  if (!c->split) return fail(c, DS_ERR_STATE, "ds_set_cfl_min: between ds_step_density and ds_step_complete only");
+  if (!(dtmin > 0)) return fail(c, DS_ERR_ARG, "ds_set_cfl_min: dtmin must be positive (or +inf)");
+  CK(cudaSetDevice(c->device));
+  unsigned long long bits = 0;
+  memcpy(&bits, &dtmin, sizeof(double));
+  CK(cudaMemcpyAsync(&c->d_tstate[tube].dtmin_bits, &bits, sizeof(bits), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
+}
+
+ds_status ds_set_gas_hydro(ds_ctx *c, int tube, int n, const int *idx, const double *rho, const double *p) {
+  if (!c || tube < 0 || tube >= c->ntubes || n < 0 || (n > 0 && (!idx || !rho || !p))) return DS_ERR_ARG;
+  if (!c->split) return fail(c, DS_ERR_STATE, "ds_set_gas_hydro: between ds_step_density and ds_step_complete only");
+  const TubeDesc &T = c->tdesc[tube];
+  const int ng = T.seg_end[0] - T.seg_begin[0];
+  if (n > ng) return fail(c, DS_ERR_ARG, "ds_set_gas_hydro: more entries than gas particles");
+  for (int k = 0; k < n; k++)
+    if (idx[k] < 0 || idx[k] >= ng) return fail(c, DS_ERR_ARG, "ds_set_gas_hydro: index out of range");
+  if (n == 0) return DS_OK;
+  CK(cudaSetDevice(c->device));
+  if (c->hy_cap < n) {  // once, for every gas particle of the largest tube
+    int cap = 0;
+    for (const auto &D : c->tdesc) cap = std::max(cap, D.seg_end[0] - D.seg_begin[0]);
+    DA(c->hy_idx, (size_t)cap);
+    DA(c->hy_val, 2 * (size_t)cap);
+    c->hy_cap = cap;
+  }
+  if (!c->inv) DA(c->inv, c->N ? c->N : 1);
+  CK(cudaMemcpyAsync(c->hy_idx, idx, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->hy_val, rho, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->hy_val + n, p, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  const int nch = (int)c->ch_all.size();
+  DevState st = c->buf[c->parity].view();
+  if (nch) k_inverse<<<nch, DS_CHUNK, 0, c->stream>>>(c->d_ch_all, c->d_tubes, st.pid, c->inv);
+  ds_launch_set_hydro(c->d_tubes, tube, n, c->hy_idx, c->hy_val, c->inv, st, c->cs64, c->pt64, c->hyd32, c->pos32,
+                      c->any_fp32, c->any_hpp, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return DS_OK;
+}
+
+ds_status ds_step_complete(ds_ctx *c) {
+  if (!c) return DS_ERR_ARG;
+  if (!c->split) return fail(c, DS_ERR_STATE, "ds_step_complete: no step begun (ds_step_density)");
+  CK(cudaSetDevice(c->device));
+  enqueue_rest(c, nullptr);
+  CK(cudaGetLastError());
+  c->split = 0;
+  CK(cudaStreamSynchronize(c->stream));
+  return check_flags(c);
+}
+
+ds_status ds_set_time(ds_ctx *c, int tube, double Tm, long long nsteps) {
+  if (!c || tube < 0 || tube >= c->ntubes || nsteps < 0 || !std::isfinite(Tm)) return DS_ERR_ARG;
+  if (c->split) return fail(c, DS_ERR_STATE, "ds_set_time: a split step is in progress");
+  if (!c->finalized) {
+    if (c->clock_set.empty()) c->clock_set.assign(c->ntubes, {false, {0.0, 0LL}});
+    c->clock_set[tube] = {true, {Tm, nsteps}};
+    return DS_OK;
+  }
+  TubeState ts;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&ts, c->d_tstate + tube, sizeof ts, cudaMemcpyDeviceToHost));
+  ts.Tm = Tm;
+  ts.nstep = nsteps;
+  CK(cudaMemcpy(c->d_tstate + tube, &ts, sizeof ts, cudaMemcpyHostToDevice));
+  return DS_OK;
+}
+
+ds_status ds_idic_columns(const ds_params *p, int n, const double *x, int *col) {
+  if (!p || n < 0 || (n > 0 && (!x || !col))) return DS_ERR_ARG;
+  TubeDesc T;
+  build_desc(*p, T);
+  if (!(T.aw > 0) || !std::isfinite(T.aw)) return DS_ERR_ARG;
+  const bool fast = p->precision == DS_PRECISION_FP32;
+  const bool proper = (p->mode & DS_MODE_IDIC_PROPER) != 0;
+  for (int i = 0; i < n; i++) {
+    double v;
+    if (fast) v = std::floor(std::fma(x[i], T.iaa, T.iab[0]));  // fast_idic_cell
+    else if (proper) v = std::floor((x[i] - T.ox) / T.aw);     // ds_idic_cell, proper grid
+    else v = std::trunc((x[i] - T.ox) / T.aw);                  // ds_idic_cell, the reference's int()
+    col[i] = v < -2147483647.0 ? -2147483647 : (v > 2147483647.0 ? 2147483647 : (int)v);
+  }
   return DS_OK;
 }
 

@@ -1061,6 +1061,35 @@ __global__ void k_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, 
   }
 }
 
+// Split step: the density and pressure of listed gas particles (caller
+// indices, slots through inv) set from outside between the two parts of a
+// step, with what the density sweep derives from them for the force sweep --
+// the same expressions as its epilogues (FP64: c_s, p / rho^2 and their FP32
+// copies; FP32: the FP32 inputs, 1/h of the particle).
+__global__ void k_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val,
+                            const int *inv, DevState st, double *cs64, double *pt64, float4 *hyd32,
+                            const float4 *pos32, int fp32, int hpp) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const TubeDesc &T = tubes[tube];
+  const int q = inv[T.seg_begin[0] + idx[k]];
+  const double rho = val[k], p = val[n + k];
+  st.rho[q] = rho;
+  st.p[q] = p;
+  if (fp32) {
+    const float rhof = (float)rho, pf = (float)p;
+    const float csf = sqrtf((float)T.gam * pf / rhof);
+    const float hown = hpp ? pos32[q].w : (float)T.h;
+    hyd32[q] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
+  } else {
+    const double cs = sqrt(T.gam * p / rho);
+    const double pt = p / (rho * rho);
+    cs64[q] = cs;
+    pt64[q] = pt;
+    hyd32[q] = make_float4((float)cs, (float)pt, (float)rho, 0.0f);
+  }
+}
+
 __global__ void k_fill(double *a, int n, double v) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] = v;
@@ -1120,6 +1149,13 @@ void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const
                                    force);
   }
   k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);
+}
+void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val, const int *inv,
+                         DevState st, double *cs64, double *pt64, float4 *hyd32, const float4 *pos32, bool fp32,
+                         bool hpp, cudaStream_t s) {
+  if (n > 0)
+    k_set_hydro<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, n, idx, val, inv, st, cs64, pt64, hyd32, pos32,
+                                                   fp32 ? 1 : 0, hpp ? 1 : 0);
 }
 void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s) {
   k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);

@@ -37,6 +37,17 @@ def _f64(a, n):
     return a
 
 
+def idic_columns(P: Params, x) -> np.ndarray:
+    """The IDIC cell column (x index) of each position as the step computes it
+    for P's precision (ds_idic_columns, host-side)."""
+    L = _lib.load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    col = np.empty(max(len(x), 1), dtype=np.int32)
+    cp = _lib.params_to_c(P)
+    _lib.check(L, None, L.ds_idic_columns(ctypes.byref(cp), len(x), _dp(x), _ip(col)), "ds_idic_columns")
+    return col[: len(x)]
+
+
 class Solver:
     def __init__(self, params):
         self.L = _lib.load()
@@ -94,6 +105,35 @@ class Solver:
 
     def synchronize(self):
         _lib.check(self.L, self.ctx, self.L.ds_synchronize(self.ctx), "ds_synchronize")
+
+    # -- split step (slab decomposition) -------------------------------------
+    def step_density(self):
+        """First part of one step: sort, gas density, EOS (ds_step_density)."""
+        _lib.check(self.L, self.ctx, self.L.ds_step_density(self.ctx), "ds_step_density")
+
+    def cfl_min(self, tube: int = 0) -> float:
+        v = ctypes.c_double(0.0)
+        _lib.check(self.L, self.ctx, self.L.ds_get_cfl_min(self.ctx, tube, ctypes.byref(v)), "ds_get_cfl_min")
+        return v.value
+
+    def set_cfl_min(self, tube: int, dtmin: float):
+        _lib.check(self.L, self.ctx, self.L.ds_set_cfl_min(self.ctx, tube, float(dtmin)), "ds_set_cfl_min")
+
+    def set_gas_hydro(self, tube: int, idx, rho, p):
+        """Density and pressure of gas particles (caller indices idx) between
+        the two parts of a step (ds_set_gas_hydro)."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        n = len(idx)
+        rho, p = _f64(rho, n), _f64(p, n)
+        _lib.check(self.L, self.ctx, self.L.ds_set_gas_hydro(self.ctx, tube, n, _ip(idx), _dp(rho), _dp(p)),
+                   "ds_set_gas_hydro")
+
+    def step_complete(self):
+        """Second part of the step begun by step_density (ds_step_complete)."""
+        _lib.check(self.L, self.ctx, self.L.ds_step_complete(self.ctx), "ds_step_complete")
+
+    def set_time(self, tube: int, Tm: float, nsteps: int):
+        _lib.check(self.L, self.ctx, self.L.ds_set_time(self.ctx, tube, float(Tm), int(nsteps)), "ds_set_time")
 
     # -- host arrays as the state of record ----------------------------------
     def pinned(self, n: int, dtype=np.float64) -> np.ndarray:

@@ -407,6 +407,40 @@ ds_status ds_list_stats(ds_ctx *c, int tube, long long *rebuilds, long long *ste
  * linked cell lists (kernel.cu:1937-1995) are walked afresh every step. */
 ds_status ds_debug_force_lists(ds_ctx *c, int tube, int cap, int *count, int *nbr);
 
+/* Split step, for one tube cut into x-slabs across processes (the host layer
+ * in dustyshock3d_gb300/slab.py).  A slab's context holds its own particles
+ * and frozen copies (Ind != 0) of the other slabs' gas within 2 h_max of its
+ * boundaries ("ghosts").  One step is
+ *   ds_step_density   the sort, the gas density and the EOS (and the dust
+ *                     density); the ghosts' own densities are not computed;
+ *   ds_get_cfl_min    the slab's CFL candidate min h / (c_s + |v|) over its
+ *                     updated gas (+inf without CFL);
+ *   ds_set_cfl_min    the minimum over all slabs (an allreduce(min) on the host);
+ *   ds_set_gas_hydro  the ghosts' density and pressure as their owners computed
+ *                     them (idx: caller indices of gas particles of the tube);
+ *   ds_step_complete  t_stop, the step size, the force, the IDIC cell solve,
+ *                     the update and the clock.
+ * The reference runs one domain on one device (kernel.cu:1793); its step
+ * (kernel.cu:1937-2566) is split after the density and EOS (kernel.cu:2011-2024)
+ * so the ghosts' pressure can arrive before the force (kernel.cu:2233-2266).
+ * Each call synchronises the context's stream. */
+ds_status ds_step_density(ds_ctx *c);
+ds_status ds_get_cfl_min(ds_ctx *c, int tube, double *dtmin);
+ds_status ds_set_cfl_min(ds_ctx *c, int tube, double dtmin);
+ds_status ds_set_gas_hydro(ds_ctx *c, int tube, int n, const int *idx, const double *rho, const double *p);
+ds_status ds_step_complete(ds_ctx *c);
+
+/* Set a tube's clock (time and steps taken), e.g. when a slab's state moves to
+ * a larger context.  The reference keeps Tm in its time loop (kernel.cu:1929). */
+ds_status ds_set_time(ds_ctx *c, int tube, double Tm, long long nsteps);
+
+/* Host-side: the IDIC cell column (x index) of each position, computed as the
+ * step computes it for the parameters' precision (FP64: the division of
+ * kernel.cu:2116 with the proper grid's floor; FP32: one FMA with the
+ * reciprocal width).  Slab boundaries fall on these columns, so every IDIC
+ * cell's particles live in one slab. */
+ds_status ds_idic_columns(const ds_params *p, int n, const double *x, int *col);
+
 /* Device bytes held by the context, and particles per tube. */
 ds_status ds_memory_bytes(ds_ctx *c, long long *bytes);
 
