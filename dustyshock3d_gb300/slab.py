@@ -334,6 +334,8 @@ class SolverBackend:
                 self.Tm, _, self.nstep = self.S.time(0)
                 self.S.close()
             self.cap = [int(c * self.slack) + 64 for c in counts]
+            # the reference's per-species particle limit (kernel.cu:1751) covers the capacity
+            self.Pext.Maximum_particle = max(int(self.P.Maximum_particle), max(self.cap))
             self.S = Solver(self.Pext)
             self.S.set_time(0, self.Tm, self.nstep)
         self.S.set_tube(0, [concat([s, self._park(k - s.n)]) for s, k in zip(species, self.cap)])
