@@ -738,12 +738,19 @@ def run_accuracy(args):
     of magnitude once the shock has formed (the M4 kernel at h = 1.3 dx has
     ~74 neighbours, twice that behind the shock, where SPH particle
     arrangements are unstable), so the L1 of that pair of FP64 runs is the
-    level below which no comparison of two differently rounded runs falls."""
+    level below which no comparison of two differently rounded runs falls.
+
+    Against the physics: the runs in a limit with a closed-form answer (eps =
+    0.01: Sod on the gas states; t_s = 1e-4: gas and dust as one mixture of
+    sound speed c_s / sqrt(1 + eps)) are also scored against the exact Riemann
+    solution (dustyshock3d_gb300.riemann, Toro's method), FP32 beside FP64:
+    the FP32 path meets the spec accuracy when its error against the
+    exact solution is within a stated factor of the FP64 path's."""
     import copy
 
     import numpy as np
 
-    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300 import ic, riemann
     from dustyshock3d_gb300.solver import Solver
     ws, rank, dist = dist_setup()
     if rank != 0:
@@ -788,6 +795,13 @@ def run_accuracy(args):
                    **errors(g32, d32, g64, d64, P.X_min, P.X_max),
                    "fp32_particle_steps_per_s": n * n32 / (ms32 * 1e-3),
                    "fp64_particle_steps_per_s": n * n64 / (ms64 * 1e-3)}
+            limit = "gas" if eps <= 0.01 else ("coupled" if t_s <= 1e-4 else None)
+            if limit:
+                s64 = riemann.score_dusty_sod(g64, d64, T32, eps, limit)
+                s32 = riemann.score_dusty_sod(g32, d32, T32, eps, limit)
+                row["exact"] = {"limit": limit, "fp64": s64, "fp32": s32,
+                                "fp32_over_fp64": {k: s32[k] / s64[k] for k in s64
+                                                   if k.startswith("l1_") and s64[k] > 0}}
             rows.append(row)
             print(json.dumps(row), file=sys.stderr, flush=True)
             if t_s == 1e-3 and eps == 1.0:
@@ -800,8 +814,10 @@ def run_accuracy(args):
                 print(json.dumps(floor), file=sys.stderr, flush=True)
     clk = clocks.stop()
     keys = ("l1_rho_gas", "l1_v_gas", "l1_v_dust", "l1_profile_rho_gas", "l1_profile_v_gas", "l1_profile_v_dust")
+    ratios = [v for r in rows if "exact" in r for v in r["exact"]["fp32_over_fp64"].values()]
     line = {"metric": "l1 error, fp32 path vs fp64 path", "workload": "accuracy_720k", "t_end": args.t_end,
             "particles": n, "rows": rows, "max": {k: max(r[k] for r in rows) for k in keys},
+            "exact_fp32_over_fp64": {"min": min(ratios), "max": max(ratios)} if ratios else None,
             "fp64_floor": floor,
             "note": "rates include up to 9 steps after t_end that do no work (steps run in groups of 10)",
             "clocks": clk}
