@@ -238,7 +238,8 @@ def batch64_record(seed, steps, warmup, shard=None):
     tune_s = time.perf_counter() - t0
     ps = []
     for P, _ in tubes:
-        Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth)
+        Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth, choice.persistent,
+                       choice.idic_lanes)
         Q.precision = "fp32"
         ps.append(Q)
     n = sum(sizes[i] for i in idx)
@@ -254,7 +255,8 @@ def batch64_record(seed, steps, warmup, shard=None):
            "warmup": warmup, "tubes": len(tubes), "particles": n, "seed": seed,
            "initial_conditions": "generated on the device (ds_init_tube)",
            "autotuned": dataclasses.asdict(choice), "tuning_s": tune_s,
-           "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, ms=d) for a, b, c, d in log],
+           "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, persistent=p, idic_lanes=q, ms=d)
+                          for a, b, c, p, q, d in log],
            "device_bytes": mem,
            "phase_ms_per_step": {k: v / steps for k, v in zip(("sort", "density", "force", "idic_update"), phase)},
            "gpu_launches": kps * steps}

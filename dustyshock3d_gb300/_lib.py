@@ -36,7 +36,7 @@ class DsParams(ctypes.Structure):
         ("t_empty", ctypes.c_double), ("list_depth", ctypes.c_int), ("force_list", ctypes.c_int),
         ("mass_ratio", ctypes.c_double * MAX_DUST), ("R_dust", ctypes.c_double * MAX_DUST),
         ("t_stop_const", ctypes.c_double * MAX_DUST), ("eps_empty", ctypes.c_double * MAX_DUST),
-        ("list_skin", ctypes.c_double),
+        ("list_skin", ctypes.c_double), ("persistent", ctypes.c_int), ("idic_lanes", ctypes.c_int),
     ]
 
 
@@ -155,6 +155,8 @@ def params_to_c(P: Params) -> DsParams:
     c.list_depth = int(getattr(P, "list_depth", 0) or 0)
     c.force_list = int(getattr(P, "force_list", 0) or 0)
     c.list_skin = float(getattr(P, "list_skin", 0.0) or 0.0)
+    c.persistent = int(getattr(P, "persistent", 0) or 0)
+    c.idic_lanes = int(getattr(P, "idic_lanes", 0) or 0)
     for k in range(MAX_DUST):
         c.mass_ratio[k] = float(P.mass_ratio[k]) if k < len(P.mass_ratio) else 0.0
         c.R_dust[k] = float(P.R_dust[k]) if k < len(P.R_dust) else 0.0
@@ -180,6 +182,8 @@ def params_from_c(c: DsParams) -> Params:
     P.list_depth = int(c.list_depth)
     P.force_list = int(c.force_list)
     P.list_skin = float(c.list_skin)
+    P.persistent = int(c.persistent)
+    P.idic_lanes = int(c.idic_lanes)
     P.mass_ratio = [float(c.mass_ratio[k]) for k in range(P.n_dust)]
     P.R_dust = [float(c.R_dust[k]) for k in range(P.n_dust)]
     P.t_stop_const = [float(c.t_stop_const[k]) for k in range(P.n_dust)]

@@ -112,6 +112,13 @@ struct ds_ctx {
   // ialt: the IDIC key sort's result is in the alternate buffers
   int split = 0;
   bool ialt = false;
+  // persistent FP32 sweeps (ds_params.persistent of tube 0): work counters,
+  // SMs, blocks per SM of each sweep
+  bool persistent = false;
+  int *d_work = nullptr;
+  int nsm = 0;
+  int bps[DS_NSWEEP] = {0};
+  int idic_lanes = 4;     // FP32 path: threads per IDIC key in the cell sums
   int *hy_idx = nullptr;       // ds_set_gas_hydro: caller indices, rho, p on the device
   double *hy_val = nullptr;
   int hy_cap = 0;
@@ -303,6 +310,9 @@ ds_status check_params(ds_ctx *c, const ds_params &P) {
   if (((P.mode & (DS_MODE_PERIODIC_Y | DS_MODE_PERIODIC_Z)) != 0) && !(P.mode & DS_MODE_GRID_PROPER))
     return fail(c, DS_ERR_UNSUPPORTED, "periodic axes need the proper cell grid (DS_MODE_GRID_PROPER)");
   if (!(P.list_skin >= 0 && P.list_skin <= 4)) return fail(c, DS_ERR_ARG, "list_skin must be in [0, 4]");
+  if (P.persistent != 0 && P.persistent != 1) return fail(c, DS_ERR_ARG, "persistent must be 0 or 1");
+  if (P.idic_lanes != 0 && P.idic_lanes != 2 && P.idic_lanes != 4 && P.idic_lanes != 8)
+    return fail(c, DS_ERR_ARG, "idic_lanes must be 0, 2, 4 or 8");
   {  // the grid sizes in double first: the int conversions and products of build_desc must not overflow
     const double w = P.cell_w > 0 ? P.cell_w : 2.0 * P.h;  // list reuse only widens it: fewer cells
     const double aw = P.idic_w > 0 ? P.idic_w : P.Coeff_h_dust_cell * P.h;
@@ -376,6 +386,20 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.nbl_walk = nullptr;
   a.nbl_cap = 0;
   a.reuse = 0;
+  a.work = nullptr;
+  a.nsm = 0;
+  for (int k = 0; k < DS_NSWEEP; k++) a.bps[k] = 0;
+  return a;
+}
+
+// The step's sweeps: with persistent sweeps, the work counters (zeroed by
+// k_step_begin) and the grid sizes.
+SweepArgs step_sweep_args(ds_ctx *c, SweepArgs a) {
+  if (c->persistent && c->d_work) {
+    a.work = c->d_work;
+    a.nsm = c->nsm;
+    for (int k = 0; k < DS_NSWEEP; k++) a.bps[k] = c->bps[k];
+  }
   return a;
 }
 
@@ -442,8 +466,8 @@ void enqueue_density(ds_ctx *c, cudaEvent_t *ev) {
   c->ialt = alt;
   if (ev) cudaEventRecord(ev[1], s);
   const bool fp32 = c->any_fp32;
-  SweepArgs ag = gas_sweep_args(c);
-  SweepArgs ad = sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size());
+  SweepArgs ag = step_sweep_args(c, gas_sweep_args(c));
+  SweepArgs ad = step_sweep_args(c, sweep_args(c, c->d_ch_dust, (int)c->ch_dust.size()));
   const int depth = c->params[0].list_depth;
   if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
@@ -461,7 +485,7 @@ void enqueue_rest(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullpt
                   cudaEvent_t after_force = nullptr) {
   cudaStream_t s = c->stream;
   const bool fp32 = c->any_fp32;
-  SweepArgs ag = gas_sweep_args(c);
+  SweepArgs ag = step_sweep_args(c, gas_sweep_args(c));
   const int depth = c->params[0].list_depth;
   if (after_density) cudaEventRecord(after_density, s);
   if (fp32 && c->wstream) {  // the overflow walk beside t_stop, dt and the list kernel
@@ -486,7 +510,7 @@ void enqueue_rest(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nullpt
   const uint32_t *ik = c->ialt ? c->ikalt : c->ikin;
   const uint32_t *iv = c->ialt ? c->ivalt : c->ivin;
   ds_launch_idic_reduce(ik, iv, c->N, c->nikeys, c->d_seg_key0, c->d_seg_species, c->d_seg_orphan, c->nseg, st,
-                        c->ca, fp32, s);
+                        c->ca, fp32, s, c->idic_lanes);
   ds_launch_idic_solve(c->d_tubes, c->d_tstate, c->d_tube_cell0, c->ntubes, c->ncell_total, c->ca, fp32, s);
   ds_launch_relax_move(c->d_tubes, c->d_tstate, c->d_ch_all, (int)c->ch_all.size(), st, c->idic_local, c->edot,
                        c->ca, c->d_flags, fp32, s);
@@ -503,7 +527,7 @@ void enqueue_physics(ds_ctx *c, cudaEvent_t *ev, cudaEvent_t after_density = nul
 // The start of a step: the clocks and, with list reuse, which tubes keep
 // their lists; then the sort.
 void enqueue_step_begin(ds_ctx *c) {
-  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->stream);
+  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->d_work, c->stream);
   if (c->reuse)  // which tubes keep their lists this step
     ds_launch_list_test(c->d_tubes, c->d_tstate, c->ntubes, c->d_ch_gas, (int)c->ch_gas.size(),
                         c->buf[c->parity].view(), fast_skey(c), c->pos_ref, c->disp, c->d_nseg_key0, c->d_nseg_tube,
@@ -625,7 +649,7 @@ void enqueue_bound_step(ds_ctx *c) {
   k_bound_in<1><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
   cudaEventRecord(c->e_up, s2);
   c->parity = P0 ^ 1;  // the caller-order state; the sort brings it back to P0
-  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, s);
+  ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->d_work, s);
   enqueue_sort(c, false, c->e_up);  // the host's arrays: every tube re-sorts
   if (c->reuse) ds_launch_list_decide(c->d_tubes, c->d_tstate, c->ntubes, c->d_force, c->d_any, s);
   k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->buf[c->parity].pid, c->inv);
@@ -746,6 +770,18 @@ ds_status finalize(ds_ctx *c) {
     CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->e_wjoin, cudaEventDisableTiming));
     for (const auto &T : c->tdesc) c->reuse = c->reuse || T.skin > 0.0;
+  }
+  c->persistent = c->any_fp32 && c->params[0].persistent != 0;
+  DA(c->d_work, DS_NSWEEP);
+  CK(cudaMemsetAsync(c->d_work, 0, sizeof(int) * DS_NSWEEP, c->stream));
+  if (c->persistent) {
+    CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
+    ds_sweep32_blocks_per_sm(c->any_hpp, c->params[0].list_depth, c->nbl != nullptr, c->bps);
+    CK(cudaGetLastError());
+  }
+  {
+    const int l = c->params[0].idic_lanes;
+    c->idic_lanes = (l == 2 || l == 8) ? l : 4;
   }
   if (c->reuse) {
     DA(c->pos_ref, N); DA(c->disp, N); DA(c->cellstat, (size_t)nkeys);

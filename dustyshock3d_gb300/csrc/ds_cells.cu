@@ -37,8 +37,9 @@ __device__ __forceinline__ bool finite_bits(double v) {
   return ((unsigned)__double2hiint(v) & 0x7ff00000u) != 0x7ff00000u;
 }
 
-__global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes) {
+__global__ void k_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, int *work) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (work && t < DS_NSWEEP) work[t] = 0;  // the persistent sweeps' chunk counters
   if (t >= ntubes) return;
   ts[t].active = ts[t].Tm < tubes[t].t_end ? 1 : 0;
   ts[t].dtmin_bits = dbl_bits(__longlong_as_double(0x7ff0000000000000LL));  // +inf
@@ -1107,8 +1108,9 @@ __global__ void k_iota(int *a, int n) {
 // ---------------------------------------------------------------------------
 static inline int blocks_for(int n, int b) { return (n + b - 1) / b; }
 
-void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s) {
-  k_step_begin<<<blocks_for(ntubes, 64), 64, 0, s>>>(tubes, ts, ntubes);
+void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, int *work, cudaStream_t s) {
+  const int n = ntubes > DS_NSWEEP ? ntubes : DS_NSWEEP;
+  k_step_begin<<<blocks_for(n, 64), 64, 0, s>>>(tubes, ts, ntubes, work);
 }
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
                     uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts, const uint32_t *prev_skey) {
@@ -1160,17 +1162,25 @@ void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx,
 void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s) {
   k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);
 }
-#ifndef DS_IDIC_LANES
-#define DS_IDIC_LANES 4  // lanes per IDIC key of the FP32 path's cell sums (measured: 4 beats 8)
-#endif
+// FP32 path: lanes per IDIC key of the cell sums, 2, 4 or 8 (an autotuner
+// choice; 4 measured fastest on the 720k tube)
+template <int LANES>
+static void launch_idic_split(const uint32_t *islot, int nikeys, const int *seg_key0, const int *seg_species,
+                              const int *seg_orphan, int nseg, DevState st, CellArrays ca, cudaStream_t s) {
+  k_idic_reduce_split<LANES><<<(int)(((long long)LANES * nikeys + 127) / 128), 128, 0, s>>>(
+      islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca);
+}
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
-                           bool fast, cudaStream_t s) {
+                           bool fast, cudaStream_t s, int lanes) {
   if (nikeys <= 0) return;
   k_cell_start<<<blocks_for(n + 1, 256), 256, 0, s>>>(ikey, n, nikeys, ca.start, nullptr);
-  if (fast)
-    k_idic_reduce_split<DS_IDIC_LANES><<<(int)(((long long)DS_IDIC_LANES * nikeys + 127) / 128), 128, 0, s>>>(
-        islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca);
+  if (fast && lanes == 2)
+    launch_idic_split<2>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca, s);
+  else if (fast && lanes == 8)
+    launch_idic_split<8>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca, s);
+  else if (fast)
+    launch_idic_split<4>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg, st, ca, s);
   else
     k_idic_reduce<<<blocks_for(nikeys, 128), 128, 0, s>>>(islot, nikeys, seg_key0, seg_species, seg_orphan, nseg,
                                                           st, ca);

@@ -582,6 +582,14 @@ __device__ __forceinline__ double ds_diff(double xj, double s, double xi) {
 }
 
 // Arguments shared by the sweep kernels.
+// FP32 sweeps with a work counter each (SweepArgs::work + the index)
+#define DS_SW_DENSITY 0
+#define DS_SW_DENSITY_LST 1
+#define DS_SW_DUST_DENSITY 2
+#define DS_SW_FORCE_LIST 3
+#define DS_SW_FORCE_WALK 4
+#define DS_NSWEEP 5
+
 struct SweepArgs {
   const TubeDesc *tubes;
   const TubeState *tstate;
@@ -613,4 +621,11 @@ struct SweepArgs {
   // list reuse: a tube whose TubeState::rebuild is 0 this step keeps the lists
   // (and slot order) of its last re-sort; 0: every step re-sorts and records
   int reuse;
+  // persistent sweeps: nullptr -> one block per chunk; else the FP32 sweeps
+  // run on a grid of about as many blocks as fit on the GPU at once, each
+  // claiming its next chunk from work[k] (k: the sweep's counter, zeroed by
+  // k_step_begin)
+  int *work;
+  int nsm;
+  int bps[DS_NSWEEP];  // blocks per SM that fit, per sweep (the persistent grid: nsm x bps)
 };

@@ -128,9 +128,9 @@ ds_status apply_param_extension(ds_params *p, const std::string &key, const std:
       for (int q = 0; q < DS_MAX_DUST; q++) lists[l][q] = vals[q];
       return DS_OK;
     }
-  int *ints[] = {&p->n_dust, &p->stencil, &p->list_depth, &p->force_list};
-  const char *int_names[] = {"n_dust", "stencil", "list_depth", "force_list"};
-  for (int q = 0; q < 4; q++)
+  int *ints[] = {&p->n_dust, &p->stencil, &p->list_depth, &p->force_list, &p->persistent, &p->idic_lanes};
+  const char *int_names[] = {"n_dust", "stencil", "list_depth", "force_list", "persistent", "idic_lanes"};
+  for (int q = 0; q < 6; q++)
     if (key == int_names[q]) return parse_int(val, ints[q]) ? DS_OK : DS_ERR_ARG;
   if (key == "precision") {
     const std::string v = lower(trim(val));

@@ -20,7 +20,8 @@ struct CellArrays {
   int *start;               // first sorted IDIC slot of every key (run bounds)
 };
 
-void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, cudaStream_t s);
+// also zeroes the persistent sweeps' chunk counters (work: DS_NSWEEP ints, or nullptr)
+void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, int *work, cudaStream_t s);
 // fast: FP32 path (reciprocal-multiply cell indices, slot-order scatters);
 // otherwise the reference's divisions and caller-index order.
 // List reuse (FP32 path): reuse_ts != nullptr gives each tube's decision of the
@@ -53,7 +54,7 @@ void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx,
 void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s);
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,
                            const int *seg_species, const int *seg_orphan, int nseg, DevState st, CellArrays ca,
-                           bool fast, cudaStream_t s);
+                           bool fast, cudaStream_t s, int lanes = 4);
 void ds_launch_idic_solve(const TubeDesc *tubes, const TubeState *ts, const int *tube_cell0, int ntubes,
                           int ncell_total, CellArrays ca, bool fast, cudaStream_t s);
 void ds_launch_relax_move(const TubeDesc *tubes, const TubeState *ts, const Chunk *chunks, int nchunks,
@@ -85,6 +86,8 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
 void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);
 void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s);
 void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_t s);
+// blocks per SM of each FP32 sweep (DS_SW_*) for the persistent grids
+void ds_sweep32_blocks_per_sm(bool hpp, int depth, bool list, int *bps);
 // list reuse: the density of tubes keeping their lists, streamed from them
 void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s);
 // parity hook: one tube's recorded force lists by caller index (a: gas chunks)

@@ -82,6 +82,23 @@ __device__ __forceinline__ void density_epilogue(const SweepArgs &a, const TubeD
   }
 }
 
+// The chunks a block takes: blockIdx.x, then every gridDim.x-th (one block per
+// chunk), or, with a work counter (a persistent grid), the next unclaimed one
+// each time, so that blocks that finish early take more.  Every thread of the
+// block calls it once per chunk (it holds two block barriers).
+__device__ __forceinline__ int claim_chunk(int *work, int *claim) {
+  __syncthreads();  // the previous claim is read by every thread
+  if (threadIdx.x == 0) *claim = atomicAdd(work, 1);
+  __syncthreads();
+  return *claim;
+}
+__device__ __forceinline__ int first_chunk(const SweepArgs &a, int *claim) {
+  return a.work ? claim_chunk(a.work, claim) : (int)blockIdx.x;
+}
+__device__ __forceinline__ int next_chunk(const SweepArgs &a, int c, int *claim) {
+  return a.work ? claim_chunk(a.work, claim) : c + (int)gridDim.x;
+}
+
 // The 4 warp flags of a chunk as one word (nbl_walk is 4-byte aligned per chunk).
 __device__ __forceinline__ uint32_t chunk_walk_flags(const SweepArgs &a, int c) {
   return *reinterpret_cast<const uint32_t *>(a.nbl_walk + (size_t)c * (DS_SWEEP_THREADS / 32));
@@ -107,7 +124,8 @@ template <bool HPP, int WHAT, int CAP, bool LIST>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (WHAT ? 9 : 8)) k_density32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   __shared__ float4 shtab[DS_NOFS32];
-  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+  __shared__ int claim;
+  for (int c = first_chunk(a, &claim); c < a.nchunks; c = next_chunk(a, c, &claim)) {
     const Chunk ch = a.chunks[c];
     const bool record = !LIST || !a.reuse || a.tstate[ch.tube].rebuild;
     if (LIST && !record && chunk_walk_flags(a, c) == 0u) continue;  // uniform per block: the lists serve it
@@ -191,7 +209,8 @@ template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
-  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+  __shared__ int claim;
+  for (int c = first_chunk(a, &claim); c < a.nchunks; c = next_chunk(a, c, &claim)) {
     const Chunk ch = a.chunks[c];
     if (a.tstate[ch.tube].rebuild || chunk_walk_flags(a, c) == 0x01010101u) continue;  // uniform per block
     const int i = ch.begin + threadIdx.x;
@@ -328,7 +347,8 @@ template <bool HPP, int CAP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
   __shared__ uint32_t lst[CAP * DS_SWEEP_THREADS];
   __shared__ float4 shtab[DS_NOFS32];
-  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+  __shared__ int claim;
+  for (int c = first_chunk(a, &claim); c < a.nchunks; c = next_chunk(a, c, &claim)) {
     if (a.nbl && chunk_walk_flags(a, c) == 0u) continue;  // uniform per block
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
@@ -362,7 +382,8 @@ template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
-  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+  __shared__ int claim;
+  for (int c = first_chunk(a, &claim); c < a.nchunks; c = next_chunk(a, c, &claim)) {
     if (chunk_walk_flags(a, c) == 0x01010101u) continue;  // every warp walks instead; uniform per block
     const Chunk ch = a.chunks[c];
     const int i = ch.begin + threadIdx.x;
@@ -419,7 +440,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
 // entry beyond the lists' capacity); nbr[i * cap + k]: the caller index of its
 // k-th entry (k < min(count[i], cap)).
 __global__ void k_debug_force_lists(SweepArgs a, int tube, int cap, int *count, int *nbr) {
-  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+  __shared__ int claim;
+  for (int c = first_chunk(a, &claim); c < a.nchunks; c = next_chunk(a, c, &claim)) {
     const Chunk ch = a.chunks[c];
     const int q = ch.begin + threadIdx.x;
     if (ch.tube != tube || q >= ch.end) continue;
@@ -439,19 +461,61 @@ __global__ void k_debug_force_lists(SweepArgs a, int tube, int cap, int *count, 
 
 }  // namespace
 
+// One sweep launch: one block per chunk, or (with work counters) a
+// persistent grid of nsm x bps[k] blocks claiming chunks from counter k.
+template <class Kernel>
+static void launch_sweep(Kernel kern, const SweepArgs &a, int k, cudaStream_t s) {
+  SweepArgs b = a;
+  int n = a.nchunks;
+  if (b.work) {
+    b.work += k;
+    const long long g = (long long)(a.bps[k] > 0 ? a.bps[k] : 1) * (a.nsm > 0 ? a.nsm : 1);
+    n = (int)(g < n ? g : n);
+  }
+  kern<<<n, DS_SWEEP_THREADS, 0, s>>>(b);
+}
+
 template <int CAP>
 static void launch_density32(const SweepArgs &a, bool hpp, int what, cudaStream_t s) {
-  const int n = a.nchunks, t = DS_SWEEP_THREADS;
   if (what == 0 && a.nbl) {
-    if (hpp) k_density32<true, 0, CAP, true><<<n, t, 0, s>>>(a);
-    else k_density32<false, 0, CAP, true><<<n, t, 0, s>>>(a);
+    if (hpp) launch_sweep(k_density32<true, 0, CAP, true>, a, DS_SW_DENSITY, s);
+    else launch_sweep(k_density32<false, 0, CAP, true>, a, DS_SW_DENSITY, s);
   } else if (what == 0) {
-    if (hpp) k_density32<true, 0, CAP, false><<<n, t, 0, s>>>(a);
-    else k_density32<false, 0, CAP, false><<<n, t, 0, s>>>(a);
+    if (hpp) launch_sweep(k_density32<true, 0, CAP, false>, a, DS_SW_DENSITY, s);
+    else launch_sweep(k_density32<false, 0, CAP, false>, a, DS_SW_DENSITY, s);
   } else {
-    if (hpp) k_density32<true, 1, CAP, false><<<n, t, 0, s>>>(a);
-    else k_density32<false, 1, CAP, false><<<n, t, 0, s>>>(a);
+    if (hpp) launch_sweep(k_density32<true, 1, CAP, false>, a, DS_SW_DUST_DENSITY, s);
+    else launch_sweep(k_density32<false, 1, CAP, false>, a, DS_SW_DUST_DENSITY, s);
   }
+}
+
+template <class Kernel>
+static int fit(Kernel kern) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, DS_SWEEP_THREADS, 0) != cudaSuccess) b = 1;
+  return b < 1 ? 1 : b;
+}
+
+template <int CAP>
+static void fit_all(bool hpp, bool list, int *bps) {
+  if (hpp) {
+    bps[DS_SW_DENSITY] = list ? fit(k_density32<true, 0, CAP, true>) : fit(k_density32<true, 0, CAP, false>);
+    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<true>);
+    bps[DS_SW_DUST_DENSITY] = fit(k_density32<true, 1, CAP, false>);
+    bps[DS_SW_FORCE_LIST] = fit(k_force32_list<true>);
+    bps[DS_SW_FORCE_WALK] = fit(k_force32<true, CAP>);
+  } else {
+    bps[DS_SW_DENSITY] = list ? fit(k_density32<false, 0, CAP, true>) : fit(k_density32<false, 0, CAP, false>);
+    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<false>);
+    bps[DS_SW_DUST_DENSITY] = fit(k_density32<false, 1, CAP, false>);
+    bps[DS_SW_FORCE_LIST] = fit(k_force32_list<false>);
+    bps[DS_SW_FORCE_WALK] = fit(k_force32<false, CAP>);
+  }
+}
+
+void ds_sweep32_blocks_per_sm(bool hpp, int depth, bool list, int *bps) {
+  if (depth >= 64) fit_all<64>(hpp, list, bps);
+  else fit_all<32>(hpp, list, bps);
 }
 
 void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cudaStream_t s) {
@@ -462,13 +526,15 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
 
 void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s) {
   if (!a.nchunks || !a.nbl || !a.reuse) return;
-  if (hpp) k_density32_lst<true><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
-  else k_density32_lst<false><<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a);
+  if (hpp) launch_sweep(k_density32_lst<true>, a, DS_SW_DENSITY_LST, s);
+  else launch_sweep(k_density32_lst<false>, a, DS_SW_DENSITY_LST, s);
 }
 
 void ds_launch_debug_force_lists(const SweepArgs &a, int tube, int cap, int *count, int *nbr, cudaStream_t s) {
   if (!a.nchunks || !a.nbl) return;
-  k_debug_force_lists<<<a.nchunks, DS_SWEEP_THREADS, 0, s>>>(a, tube, cap, count, nbr);
+  SweepArgs b = a;
+  b.work = nullptr;  // one block per chunk
+  k_debug_force_lists<<<b.nchunks, DS_SWEEP_THREADS, 0, s>>>(b, tube, cap, count, nbr);
 }
 
 // With recorded lists: the list kernel, then the walk over overflowed chunks.
@@ -480,9 +546,8 @@ void ds_launch_force32(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) 
 // The list kernel alone (no-op without recorded lists).
 void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s) {
   if (!a.nchunks || !a.nbl) return;
-  const int n = a.nchunks, t = DS_SWEEP_THREADS;
-  if (hpp) k_force32_list<true><<<n, t, 0, s>>>(a);
-  else k_force32_list<false><<<n, t, 0, s>>>(a);
+  if (hpp) launch_sweep(k_force32_list<true>, a, DS_SW_FORCE_LIST, s);
+  else launch_sweep(k_force32_list<false>, a, DS_SW_FORCE_LIST, s);
 }
 
 // The walk: every particle without recorded lists, else only the warps the
@@ -490,12 +555,11 @@ void ds_launch_force32_list(const SweepArgs &a, bool hpp, cudaStream_t s) {
 // two may run concurrently).
 void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_t s) {
   if (!a.nchunks) return;
-  const int n = a.nchunks, t = DS_SWEEP_THREADS;
   if (depth >= 64) {
-    if (hpp) k_force32<true, 64><<<n, t, 0, s>>>(a);
-    else k_force32<false, 64><<<n, t, 0, s>>>(a);
+    if (hpp) launch_sweep(k_force32<true, 64>, a, DS_SW_FORCE_WALK, s);
+    else launch_sweep(k_force32<false, 64>, a, DS_SW_FORCE_WALK, s);
   } else {
-    if (hpp) k_force32<true, 32><<<n, t, 0, s>>>(a);
-    else k_force32<false, 32><<<n, t, 0, s>>>(a);
+    if (hpp) launch_sweep(k_force32<true, 32>, a, DS_SW_FORCE_WALK, s);
+    else launch_sweep(k_force32<false, 32>, a, DS_SW_FORCE_WALK, s);
   }
 }

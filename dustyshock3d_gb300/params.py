@@ -97,6 +97,8 @@ class Params:
     list_depth: int = 0   # FP32 sweeps: candidate-list entries per thread (0 -> 32; 64)
     force_list: int = 0   # FP32: recorded force neighbours per gas particle (0 -> 256; -1 -> off)
     list_skin: float = 0.0  # FP32 with force lists: reuse the lists across steps, skin in units of h (0 -> off)
+    persistent: int = 0   # FP32: neighbour sweeps on a persistent grid claiming chunks (1) or a block per chunk (0)
+    idic_lanes: int = 0   # FP32: threads per IDIC cell in its cell sums, 2, 4 or 8 (0 -> 4)
     precision: str = "fp64"  # "fp64" or "fp32" (FP32 neighbour sums, FP64 state/IDIC)
     mode: Mode = field(default_factory=Mode)
 
@@ -166,7 +168,7 @@ def parse_init_txt(text: str) -> Params:
             setattr(P.mode, key[5:], val.lower() in ("1", "true", "yes", "on"))
         elif key in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             setattr(P, key, [float(v) for v in val.replace(",", " ").split()])
-        elif key in ("n_dust", "stencil", "list_depth", "force_list"):
+        elif key in ("n_dust", "stencil", "list_depth", "force_list", "persistent", "idic_lanes"):
             setattr(P, key, int(val))
         elif key == "precision":
             P.precision = val
@@ -194,6 +196,8 @@ def write_init_txt(P: Params, extensions: bool = True) -> str:
         out.append(f"stencil = {P.stencil}")
         out.append(f"list_depth = {P.list_depth}")
         out.append(f"force_list = {P.force_list}")
+        out.append(f"persistent = {P.persistent}")
+        out.append(f"idic_lanes = {P.idic_lanes}")
         for k in ("mass_ratio", "R_dust", "t_stop_const", "eps_empty"):
             out.append(f"{k} = " + " ".join(repr(float(v)) for v in getattr(P, k)))
         out.append(f"precision = {P.precision}")

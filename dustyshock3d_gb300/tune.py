@@ -7,10 +7,15 @@ physics):
     (each cell walks only as many as its particles' cut-offs reach; smaller
     cells screen fewer candidates per pair, in more rows);
   * list depth: candidate-list entries per thread (32 or 64), i.e. how many
-    screened neighbours a thread stages before the pair work runs.
+    screened neighbours a thread stages before the pair work runs;
+  * persistent sweeps: one block per chunk of 128 particles, or a grid of as
+    many blocks as fit on the GPU at once, each claiming its next chunk;
+  * threads per IDIC cell in the cell sums (2, 4 or 8).
 
 The tuner times a few steps of each candidate on a sample of the batch (the
-first ``sample`` tubes) with CUDA events and returns the fastest.
+first ``sample`` tubes) with CUDA events and returns the fastest: first over
+(stencil, cell width, list depth), then, for the winner, over (persistent,
+threads per IDIC cell).
 """
 from __future__ import annotations
 
@@ -30,6 +35,8 @@ CANDIDATES = [
     (3, 0.6673, 32),
     (4, 0.5005, 32),
 ]
+# (persistent sweeps, threads per IDIC cell), tried for the best of CANDIDATES
+LAUNCH_CANDIDATES = [(0, 4), (1, 4), (0, 2), (0, 8), (1, 2), (1, 8)]
 
 
 @dataclasses.dataclass
@@ -38,13 +45,18 @@ class Choice:
     cell_factor: float
     list_depth: int
     ms_per_step: float
+    persistent: int = 0
+    idic_lanes: int = 4
 
 
-def apply(P: Params, stencil: int, cell_factor: float, list_depth: int) -> Params:
+def apply(P: Params, stencil: int, cell_factor: float, list_depth: int, persistent: int = 0,
+          idic_lanes: int = 4) -> Params:
     Q = P.copy()
     Q.stencil = stencil
     Q.cell_w = cell_factor * Q.h  # Q.h is the tube's largest smoothing length
     Q.list_depth = list_depth
+    Q.persistent = persistent
+    Q.idic_lanes = idic_lanes
     return Q
 
 
@@ -68,10 +80,21 @@ def put_tube(S: Solver, t: int, src) -> None:
         S.set_tube(t, src)
 
 
+def _time(sub, ps, warmup, steps) -> float:
+    with Solver(ps) as S:
+        for t, (_, sp) in enumerate(sub):
+            put_tube(S, t, sp)
+        S.step(warmup)
+        return S.step_timed_graph(steps) / steps  # as ds_step runs the batch: its captured graphs
+
+
 def tune(tubes: Sequence[Tuple[Params, Union[List[Species], DeviceIC]]], sample: int = 8, warmup: int = 2,
-         steps: int = 3, precision: str = "fp32", candidates=CANDIDATES) -> Tuple[Choice, list]:
+         steps: int = 3, precision: str = "fp32", candidates=CANDIDATES,
+         launch_candidates=LAUNCH_CANDIDATES) -> Tuple[Choice, list]:
     """tubes: (params, particles) pairs, the particles a species list or a
-    DeviceIC generator."""
+    DeviceIC generator.  The log holds (stencil, cell factor, list depth,
+    persistent, threads per IDIC cell, ms per step or None when the grid does
+    not fit)."""
     sub = list(tubes[:sample])
     log = []
     best = None
@@ -80,15 +103,22 @@ def tune(tubes: Sequence[Tuple[Params, Union[List[Species], DeviceIC]]], sample:
         for q in ps:
             q.precision = precision
         if not all(_fits(q) for q in ps):
-            log.append((stencil, factor, depth, None))
+            log.append((stencil, factor, depth, 0, 4, None))
             continue
-        with Solver(ps) as S:
-            for t, (_, sp) in enumerate(sub):
-                put_tube(S, t, sp)
-            S.step(warmup)
-            ms = S.step_timed_graph(steps)  # as ds_step runs the batch: its captured graphs
-        ms /= steps
-        log.append((stencil, factor, depth, ms))
+        ms = _time(sub, ps, warmup, steps)
+        log.append((stencil, factor, depth, 0, 4, ms))
         if best is None or ms < best.ms_per_step:
             best = Choice(stencil, factor, depth, ms)
+    if best is None or precision != "fp32":
+        return best, log
+    for persistent, lanes in launch_candidates:
+        if (persistent, lanes) == (0, 4):
+            continue  # timed above
+        ps = [apply(P, best.stencil, best.cell_factor, best.list_depth, persistent, lanes) for P, _ in sub]
+        for q in ps:
+            q.precision = precision
+        ms = _time(sub, ps, warmup, steps)
+        log.append((best.stencil, best.cell_factor, best.list_depth, persistent, lanes, ms))
+        if ms < best.ms_per_step:
+            best = Choice(best.stencil, best.cell_factor, best.list_depth, ms, persistent, lanes)
     return best, log

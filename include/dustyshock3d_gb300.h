@@ -141,6 +141,15 @@ typedef struct ds_params {
                                 widened so that the recorded cut-off stays within the
                                 stencil.  Ignored (off) on the FP64 path, without force
                                 lists, and with DS_MODE_DUST_RHO. */
+  int persistent;            /* FP32 path: 1 -> the neighbour sweeps run on a persistent grid
+                                (as many 128-thread blocks as fit on the GPU at once), each
+                                block claiming its next chunk of particles from a counter;
+                                0 -> one block per chunk.  An autotuner choice (batch-wide:
+                                tube 0's); results are the same either way. */
+  int idic_lanes;            /* FP32 path: threads per IDIC cell in its cell sums, 2, 4 or 8
+                                (0 -> 4); an autotuner choice (batch-wide: tube 0's); each
+                                lane sums a contiguous part in order, so a tube's result
+                                depends on it but not on its batch. */
 } ds_params;
 
 typedef struct ds_ctx ds_ctx;

@@ -39,7 +39,32 @@ def test_autotuner_keeps_the_fastest_candidate():
     tubes = [ic.uneven_tube(**ic.draw_tube_params(rng, (2.0e4, 4.0e4))) for _ in range(2)]
     best, log = tune.tune(tubes, sample=2, warmup=1, steps=2,
                           candidates=[(2, 1.001, 32), (1, 2.002, 32), (4, 0.5005, 32)])
-    timed = [row for row in log if row[3] is not None]
+    timed = [row for row in log if row[5] is not None]
     assert timed, log
-    assert best.ms_per_step == min(row[3] for row in timed)
-    assert (best.stencil, best.cell_factor) in [(row[0], row[1]) for row in timed]
+    assert best.ms_per_step == min(row[5] for row in timed)
+    assert (best.stencil, best.cell_factor, best.persistent, best.idic_lanes) in \
+        [(row[0], row[1], row[3], row[4]) for row in timed]
+    # the launch shapes were tried for the winning grid
+    assert {(row[3], row[4]) for row in timed} >= set(tune.LAUNCH_CANDIDATES)
+
+
+@pytest.mark.parametrize("persistent,lanes", [(1, 4), (0, 2), (1, 8)])
+def test_launch_shapes_keep_the_results(persistent, lanes):
+    """Persistent sweeps give the same results bit for bit (a chunk's work does
+    not depend on the block that claims it); the threads per IDIC cell change
+    only the cell sums' rounding (FP32 path bounds)."""
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.25, eps=1.0, t_s=1e-3, x_range=(-0.25, 0.25))
+    P.precision = "fp32"
+    out = []
+    for q in (P, tune.apply(P, P.stencil, P.cell_w / P.h, P.list_depth, persistent, lanes)):
+        with Solver(q) as S:
+            S.set_tube(0, sp)
+            S.step(8)
+            out.append([S.get_species(0, s) for s in range(2)])
+    for s in range(2):
+        for f in ("x", "vx", "rho"):
+            a, b = getattr(out[1][s], f), getattr(out[0][s], f)
+            if lanes == 4:
+                assert np.array_equal(a, b), (s, f)
+            else:  # the FP32 path's bounds: relative L1 1e-5
+                assert np.abs(a - b).sum() <= 1e-5 * np.abs(b).sum(), (s, f)
