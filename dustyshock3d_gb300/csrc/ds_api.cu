@@ -97,7 +97,7 @@ struct ds_ctx {
   double *origins = nullptr;  // FP32 path: TubeDesc::orig of every tube
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
-  float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr, *rec32 = nullptr;
+  float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
   double *cs64 = nullptr, *pt64 = nullptr, *dwn64 = nullptr, *edot = nullptr;
   uint32_t *nbl = nullptr;  // FP32 force neighbour lists, nbl_cap entries per gas slot of each chunk
   int *nbl_cnt = nullptr;
@@ -368,7 +368,6 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.pos32 = c->pos32;
   a.vm32 = c->vm32;
   a.hyd32 = c->hyd32;
-  a.rec32 = c->rec32;
   a.cs64 = c->cs64;
   a.pt64 = c->pt64;
   a.dwn64 = c->dwn64;
@@ -766,7 +765,6 @@ ds_status finalize(ds_ctx *c) {
     c->nbl_cap = c->params[0].force_list > 0 ? c->params[0].force_list : (skin ? 512 : 256);
     DA(c->nbl, c->ch_gas.size() * (size_t)c->nbl_cap * DS_CHUNK);
     DA(c->nbl_cnt, N);
-    DA(c->rec32, 3 * (size_t)N);
     DA(c->nbl_walk, c->ch_gas.size() * (DS_SWEEP_THREADS / 32));
     CK(cudaStreamCreateWithFlags(&c->wstream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
@@ -1600,7 +1598,7 @@ ds_status ds_set_gas_hydro(ds_ctx *c, int tube, int n, const int *idx, const dou
   DevState st = c->buf[c->parity].view();
   if (nch) k_inverse<<<nch, DS_CHUNK, 0, c->stream>>>(c->d_ch_all, c->d_tubes, st.pid, c->inv);
   ds_launch_set_hydro(c->d_tubes, tube, n, c->hy_idx, c->hy_val, c->inv, st, c->cs64, c->pt64, c->hyd32, c->pos32,
-                      c->any_fp32, c->any_hpp, c->stream, c->any_fp32 ? c->rec32 : nullptr);
+                      c->any_fp32, c->any_hpp, c->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
   return DS_OK;

@@ -1069,7 +1069,7 @@ __global__ void k_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, 
 // copies; FP32: the FP32 inputs, 1/h of the particle).
 __global__ void k_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val,
                             const int *inv, DevState st, double *cs64, double *pt64, float4 *hyd32,
-                            const float4 *pos32, int fp32, int hpp, float4 *rec32) {
+                            const float4 *pos32, int fp32, int hpp) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const TubeDesc &T = tubes[tube];
@@ -1082,7 +1082,6 @@ __global__ void k_set_hydro(const TubeDesc *tubes, int tube, int n, const int *i
     const float csf = sqrtf((float)T.gam * pf / rhof);
     const float hown = hpp ? pos32[q].w : (float)T.h;
     hyd32[q] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
-    if (rec32) rec32[3 * (size_t)q + 2] = hyd32[q];
   } else {
     const double cs = sqrt(T.gam * p / rho);
     const double pt = p / (rho * rho);
@@ -1155,10 +1154,10 @@ void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const
 }
 void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val, const int *inv,
                          DevState st, double *cs64, double *pt64, float4 *hyd32, const float4 *pos32, bool fp32,
-                         bool hpp, cudaStream_t s, float4 *rec32) {
+                         bool hpp, cudaStream_t s) {
   if (n > 0)
     k_set_hydro<<<blocks_for(n, 256), 256, 0, s>>>(tubes, tube, n, idx, val, inv, st, cs64, pt64, hyd32, pos32,
-                                                   fp32 ? 1 : 0, hpp ? 1 : 0, rec32);
+                                                   fp32 ? 1 : 0, hpp ? 1 : 0);
 }
 void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s) {
   k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);

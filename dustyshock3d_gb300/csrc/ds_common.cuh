@@ -600,8 +600,6 @@ struct SweepArgs {
   const float4 *pos32;      // prefilter / FP32 coordinates + h
   const float4 *vm32;       // FP32 vx, vy, vz, m
   float4 *hyd32;            // FP32 c, p/rho^2, rho, (unused) -- written by density
-  float4 *rec32;            // FP32 path with force lists: per gas slot 3 float4 (pos32, vm32, hyd32),
-                            // written by the density epilogue: one record per list entry for the force
   double *cs64;             // sqrt(gam p / rho) per gas slot -- written by density
   double *pt64;             // p / (rho rho) per gas slot     -- written by density
   double *dwn64;            // dW normalisation c/h^4 per gas slot -- written by density

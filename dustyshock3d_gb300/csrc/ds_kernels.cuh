@@ -49,7 +49,7 @@ void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const
 // val = rho[0..n) then p[0..n)), with the force sweep's per-particle inputs
 void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val, const int *inv,
                          DevState st, double *cs64, double *pt64, float4 *hyd32, const float4 *pos32, bool fp32,
-                         bool hpp, cudaStream_t s, float4 *rec32 = nullptr);
+                         bool hpp, cudaStream_t s);
 // the decision alone (with *force set: every tube re-sorts)
 void ds_launch_list_decide(const TubeDesc *tubes, TubeState *ts, int ntubes, int *force, int *any, cudaStream_t s);
 void ds_launch_idic_reduce(const uint32_t *ikey, const uint32_t *islot, int n, int nikeys, const int *seg_key0,

@@ -72,15 +72,8 @@ __device__ __forceinline__ void density_epilogue(const SweepArgs &a, const TubeD
     const float rhof = (float)rho, pf = (float)p;
     const float csf = sqrtf((float)T.gam * pf / rhof);
     // .w: 1/h of the particle (frozen ones too: they are force partners)
-    const float4 pos = a.pos32[i];
-    const float hown = HPP ? pos.w : (float)T.h;
-    const float4 hy = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
-    a.hyd32[i] = hy;
-    if (a.rec32) {  // the force list kernel's record of this particle
-      a.rec32[3 * (size_t)i] = pos;
-      a.rec32[3 * (size_t)i + 1] = a.vm32[i];
-      a.rec32[3 * (size_t)i + 2] = hy;
-    }
+    const float hown = HPP ? a.pos32[i].w : (float)T.h;
+    a.hyd32[i] = make_float4(csf, pf / (rhof * rhof), rhof, 1.0f / hown);
     if (upd && (T.mode & M_CFL)) {
       const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
       const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
@@ -415,10 +408,10 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) 
 #pragma unroll
       for (int t = 0; t < DS_FPIECE; t++)
         if (e + t < cnt) {
-          const size_t j = 3 * (size_t)(sb + (int)(ent[t] & DS_SLOT32_MASK));
-          pj[t] = a.rec32[j];  // one 48-byte record: two sectors for the three loads
-          vmj[t] = a.rec32[j + 1];
-          hyj[t] = a.rec32[j + 2];
+          const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
+          pj[t] = a.pos32[j];
+          vmj[t] = a.vm32[j];
+          hyj[t] = a.hyd32[j];
         }
       uint32_t nxt[DS_FPIECE];
 #pragma unroll
