@@ -55,11 +55,13 @@ __device__ __forceinline__ float r2_of(float dx, float dy, float dz) {
 }
 
 // After the density sum of particle i: the density (kernel normalisation in
-// FP64), the EOS, and the force sweep's FP32 inputs and CFL bound.
+// FP64), the EOS, and the force sweep's FP32 inputs.  Returns the particle's
+// CFL bound h / (c_s + |v|) as FP32 bits, or ~0u when it has none.
 template <bool HPP, int WHAT>
-__device__ __forceinline__ void density_epilogue(const SweepArgs &a, const TubeDesc &T, const Chunk &ch, int i,
-                                                 bool upd, bool zero, double rho, double hd, float hf,
-                                                 const Kahan &sum) {
+__device__ __forceinline__ unsigned density_epilogue(const SweepArgs &a, const TubeDesc &T, const Chunk &ch, int i,
+                                                     bool upd, bool zero, double rho, double hd, float hf,
+                                                     const Kahan &sum) {
+  unsigned dtb = ~0u;
   if (upd) rho = rho + (((double)1 / (DS_PI_REF)) / (hd * hd * hd)) * sum.value();
   if (zero || upd) a.st.rho[i] = rho;
   if (WHAT == 0) {
@@ -77,9 +79,22 @@ __device__ __forceinline__ void density_epilogue(const SweepArgs &a, const TubeD
     if (upd && (T.mode & M_CFL)) {
       const float vx = (float)a.st.vx[i], vy = (float)a.st.vy[i], vz = (float)a.st.vz[i];
       const float dt = hf / (csf + sqrtf(vx * vx + vy * vy + vz * vz));
-      atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong((double)dt));
+      dtb = __float_as_uint(dt);
     }
   }
+  return dtb;
+}
+
+// The CFL minimum of a tube: the smallest bound of the warp's particles (FP32
+// bits: positive floats order as unsigned, NaN and negative values above
+// them), then one atomic per warp, as a double -- the value a per-particle
+// atomic would leave, with 1/32 of the atomics on the tube's one address
+// (per-particle atomics there serialised and took a large part of the sweep).
+// Every lane of the warp calls it (a warp's lanes share their chunk's tube).
+__device__ __forceinline__ void cfl_min_warp(const SweepArgs &a, int tube, unsigned dtb) {
+  const unsigned m = __reduce_min_sync(0xffffffffu, dtb);
+  if ((threadIdx.x & 31) == 0 && m != ~0u)
+    atomicMin(&a.tstate_rw[tube].dtmin_bits, (unsigned long long)__double_as_longlong((double)__uint_as_float(m)));
 }
 
 // The chunks a block takes: blockIdx.x, then every gridDim.x-th (one block per
@@ -191,8 +206,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
       if ((threadIdx.x & 31) == 0) a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)] = over != 0u;
       if (i < ch.end) a.nbl_cnt[i] = cnt;
     }
-    if (!valid) continue;
-    density_epilogue<HPP, WHAT>(a, T, ch, i, upd, zero, rho, hd, hf, sum);
+    const unsigned dtb = valid ? density_epilogue<HPP, WHAT>(a, T, ch, i, upd, zero, rho, hd, hf, sum) : ~0u;
+    if (WHAT == 0) cfl_min_warp(a, ch.tube, dtb);
   }
 }
 
@@ -263,8 +278,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a)
 #pragma unroll
       for (int t = 0; t < DS_DPIECE; t++) ent[t] = nxt[t];
     }
-    if (!valid) continue;
-    density_epilogue<HPP, 0>(a, T, ch, i, upd, upd, rho, hd, hf, sum);
+    const unsigned dtb = valid ? density_epilogue<HPP, 0>(a, T, ch, i, upd, upd, rho, hd, hf, sum) : ~0u;
+    cfl_min_warp(a, ch.tube, dtb);
   }
 }
 

@@ -95,9 +95,9 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
           rho_tmp = rho_tmp + a.st.m[j] * ds_W_n(d, hi, wn);
         });
     rho = rho + rho_tmp;
-    if (!valid) continue;
-    if (zero || upd) a.st.rho[i] = rho;
-    if (WHAT == 0) {
+    unsigned long long dtb = ~0ull;  // CFL bound as double bits (positive doubles order as unsigned)
+    if (valid && (zero || upd)) a.st.rho[i] = rho;
+    if (valid && WHAT == 0) {
       // PKernel (kernel.cu:107-123) and per-particle quantities of the force sweep
       double p = a.st.p[i];
       if (upd) {
@@ -115,9 +115,15 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density64(SweepArgs a) {
         const double v = sqrt(vx * vx + vy * vy + vz * vz);
         const double hh = HPP ? a.st.h[i] : T.h;
         const double dt = hh / (cs + v);
-        atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, (unsigned long long)__double_as_longlong(dt));
+        dtb = (unsigned long long)__double_as_longlong(dt);
       }
     }
+    // one atomic per warp on the tube's CFL minimum (a warp's lanes share a tube)
+    for (int k = 16; k > 0; k >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, dtb, k);
+      dtb = o < dtb ? o : dtb;
+    }
+    if (WHAT == 0 && (threadIdx.x & 31) == 0 && dtb != ~0ull) atomicMin(&a.tstate_rw[ch.tube].dtmin_bits, dtb);
   }
 }
 
