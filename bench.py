@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 
 # Batched and served workloads (not the default line): 64 seeded uneven tubes,
 # and a Poisson stream of such tubes under a 150 GB budget.
-EXTRA_WORKLOADS = ("batch64", "serve", "accuracy_720k", "initial_conditions")
+EXTRA_WORKLOADS = ("batch64", "serve", "accuracy_720k", "initial_conditions", "reference_init")
 
 WORKLOADS = {
     # name: (dx_left, Ly, description)
@@ -190,11 +190,17 @@ def balanced_shards(sizes, ws):
 # CPU: the oracle (reference algorithm restated, FP64, OpenMP)
 # ---------------------------------------------------------------------------
 def time_cpu(name, steps, budget_s=25.0):
-    """Oracle steps on all host cores; shrinks the tube cross-section if one
-    step would not fit the budget.  Returns (particle-steps/s, sample text)."""
+    """Oracle steps on all host cores on one of the benchmark tubes.  Returns
+    (particle-steps/s, sample text, particles)."""
+    P, sp = make_tube(name, 1.0)
+    return time_cpu_params(P, sp, steps, budget_s)
+
+
+def time_cpu_params(P, sp, steps, budget_s=25.0):
+    """Oracle steps on all host cores from the given state: at least one, more
+    while they fit the budget.  Returns (particle-steps/s, sample text,
+    particles)."""
     from oracle.oracle import OracleState
-    scale = 1.0
-    P, sp = make_tube(name, scale)
     O = OracleState(P, sp)
     t0 = time.perf_counter()
     O.step(1)
@@ -445,45 +451,54 @@ def e2e_run(P, sp, steps, warmup, bound=True):
     L = _lib.load()
     S = Solver(P)
     S.set_tube(0, sp)
-    g, d = sp[0].copy().fill_missing(), sp[1].copy().fill_missing()
+    g = sp[0].copy().fill_missing()
+    ds = [q.copy().fill_missing() for q in sp[1:]]  # every dust species
     GIN = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e", "m", "h")
     DIN = ("x", "y", "z", "vx", "vy", "vz", "rho", "m", "ts", "h")
     GOUT = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "rho", "p", "e")
     DOUT = ("x", "y", "z", "vx", "vy", "vz", "rho", "ts")
     gin = {f: S.pinned(g.n) for f in GIN}
-    din = {f: S.pinned(d.n) for f in DIN}
-    gind, dind = S.pinned(g.n, np.int32), S.pinned(d.n, np.int32)
+    dins = [{f: S.pinned(d.n) for f in DIN} for d in ds]
+    gind = S.pinned(g.n, np.int32)
+    dinds = [S.pinned(d.n, np.int32) for d in ds]
     for f, a in gin.items():
         a[:] = getattr(g, f)
-    for f, a in din.items():
-        a[:] = getattr(d, f)
+    for d, din, dind in zip(ds, dins, dinds):
+        for f, a in din.items():
+            a[:] = getattr(d, f)
+        dind[:] = d.ind
     gind[:] = g.ind
-    dind[:] = d.ind
-    h2d = sum(a.nbytes for a in gin.values()) + sum(a.nbytes for a in din.values()) + gind.nbytes + dind.nbytes
+    h2d = (sum(a.nbytes for a in gin.values()) + gind.nbytes
+           + sum(sum(a.nbytes for a in din.values()) + dind.nbytes for din, dind in zip(dins, dinds)))
     if bound:  # what ds_step_host writes back (dust rho and t_stop only where the step can change them)
         dout = [f for f in DOUT if (f != "rho" or P.mode.dust_rho) and (f != "ts" or not P.mode.tstop_const)]
     else:
         dout = DOUT
-    d2h = sum(gin[f].nbytes for f in GOUT) + sum(din[f].nbytes for f in dout)
+    d2h = sum(gin[f].nbytes for f in GOUT) + sum(din[f].nbytes for din in dins for f in dout)
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
     ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
     if bound:
         S.bind_host(0, 0, gin, gind)
-        S.bind_host(0, 1, din, dind)
+        for k, (din, dind) in enumerate(zip(dins, dinds)):
+            S.bind_host(0, k + 1, din, dind)
         c = S.ctx
 
         def one():
             _lib.check(L, c, L.ds_step_host(c, 1), "ds_step_host")
     else:
-        d2h += gind.nbytes + dind.nbytes  # the downloads return Ind too
+        d2h += gind.nbytes + sum(a.nbytes for a in dinds)  # the downloads return Ind too
         c = S.ctx
 
         def one():
             _lib.check(L, c, L.ds_upload_gas(c, g.n, *[dp(gin[f]) for f in GIN], ip(gind)), "upload gas")
-            _lib.check(L, c, L.ds_upload_dust(c, 1, d.n, *[dp(din[f]) for f in DIN], ip(dind)), "upload dust")
+            for k, (d, din, dind) in enumerate(zip(ds, dins, dinds)):
+                _lib.check(L, c, L.ds_upload_dust(c, k + 1, d.n, *[dp(din[f]) for f in DIN], ip(dind)),
+                           "upload dust")
             _lib.check(L, c, L.ds_step(c, 1), "step")
             _lib.check(L, c, L.ds_download_gas(c, *[dp(gin[f]) for f in GOUT], ip(gind)), "download gas")
-            _lib.check(L, c, L.ds_download_dust(c, 1, *[dp(din[f]) for f in DOUT], ip(dind)), "download dust")
+            for k, (din, dind) in enumerate(zip(dins, dinds)):
+                _lib.check(L, c, L.ds_download_dust(c, k + 1, *[dp(din[f]) for f in DOUT], ip(dind)),
+                           "download dust")
 
     for _ in range(warmup):
         one()
@@ -827,6 +842,60 @@ def run_accuracy(args):
     return 0
 
 
+def run_reference_init(args):
+    """The reference's own default run: ds_params_init (the values of its
+    Init.txt: box [-2, 2]^3, 40 particles per unit length, h = 0.1, tau = 5e-3,
+    T_end = 0.2), its generator (init_Sod_X_Dust: 323,584 gas + 2 x 323,584
+    dust), reference mode -- the reference's grid, index coupling, eps guard,
+    2-species solve, dust density every step -- on the FP64 path, which equals
+    the oracle (and so the reference program) bit for bit.  Device-resident
+    (CUDA events around the step graphs) and end to end through
+    ds_bind_host / ds_step_host; the CPU oracle on the host cores beside it.
+    The run has 40 steps in all: --warmup steps, then up to --steps of the
+    rest are timed.  This is the like-for-like GPU number for the reference's
+    own CUDA program on the same input (which cannot be built on the GPU host)
+    and for its loops built for the host (timed where the reference tree
+    exists, oracle/compare_cpu_baselines.py)."""
+    import ctypes
+
+    from dustyshock3d_gb300 import _lib, ic
+    from dustyshock3d_gb300.solver import Solver
+    ws, rank, dist = dist_setup()
+    if rank != 0:
+        return 0
+    L = _lib.load()
+    c = _lib.DsParams()
+    _lib.check(L, None, L.ds_params_init(ctypes.byref(c)), "ds_params_init")
+    P, sp = ic.init_sod_x_dust(_lib.params_from_c(c), before_first="skip")
+    n = sum(q.n for q in sp)
+    total = int(round(P.T_end / P.tau))
+    steps = max(1, min(args.steps, total - args.warmup))
+    clocks = ClockSampler(0)
+    clocks.start()
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(args.warmup)
+        ms = S.step_timed_graph(steps)
+        kps = S.kernels_per_step()
+    el, h2d, d2h = e2e_run(P, sp, steps, args.warmup, bound=True)
+    clk = clocks.stop()
+    v, sample, _ = time_cpu_params(P, sp, 1)
+    line = {"metric": "particle-steps/s", "value": n * steps / (ms * 1e-3), "unit": "particle-steps/s",
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the reference's own default initial conditions)",
+            "config": {"workload": "reference_init", "particles": n, "gas": sp[0].n,
+                       "description": "the reference's default Init.txt run, reference mode, FP64 path"},
+            "e2e": {"value": n * steps / el, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / steps,
+                    "path": "ds_bind_host + ds_step_host(1) per step, fp64 path"},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores(), "kind": "port",
+                             "sample": sample},
+            "gpu_launches": kps * steps, "clocks": clk}
+    print(json.dumps(line))
+    return 0
+
+
 def run_ic(args):
     """Initial conditions of the 720k and 5.76M tubes: made on the host (numpy,
     ic.dusty_sod_tube) and uploaded at the first step, against generated on the
@@ -897,6 +966,8 @@ def main():
         return run_serve(args)
     if args.workload == "accuracy_720k":
         return run_accuracy(args)
+    if args.workload == "reference_init":
+        return run_reference_init(args)
     if args.workload == "initial_conditions":
         return run_ic(args)
     return run_ours(args)
