@@ -976,6 +976,7 @@ __global__ void k_upload_mapped(HostFields hf, const int *ind, int n, double hde
 }
 
 ds_status set_species(ds_ctx *c, int tube, int s, int n, const double *const *fields, const int *ind) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c) return DS_ERR_ARG;
   if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
   if (s < 0 || s > c->params[tube].n_dust) return fail(c, DS_ERR_ARG, "bad species index");
@@ -1282,6 +1283,7 @@ ds_status ds_ic_plan(const ds_ic *ic, const ds_params *init, ds_params *out, int
 }
 
 ds_status ds_init_tube(ds_ctx *c, int tube, const ds_ic *ic) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c || !ic) return DS_ERR_ARG;
   if (tube < 0 || tube >= c->ntubes) return fail(c, DS_ERR_ARG, "bad tube index");
   auto plan = std::make_shared<IcPlan>();
@@ -1333,6 +1335,7 @@ ds_status ds_upload_dust(ds_ctx *c, int species, int n, const double *x, const d
 }
 
 ds_status ds_step_async(ds_ctx *c, int nsteps) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c || nsteps < 0) return DS_ERR_ARG;
   ds_status st = finalize(c);
   if (st != DS_OK) return st;
@@ -1419,6 +1422,7 @@ ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *f
 }
 
 ds_status ds_step_host(ds_ctx *c, int nsteps) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c || nsteps < 0) return DS_ERR_ARG;
   ds_status st = finalize(c);
   if (st != DS_OK) return st;
@@ -1433,6 +1437,7 @@ ds_status ds_step_host(ds_ctx *c, int nsteps) {
 }
 
 ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c || nsteps < 0) return DS_ERR_ARG;
   ds_status st = finalize(c);
   if (st != DS_OK) return st;
@@ -1489,6 +1494,7 @@ ds_status ds_step_timed(ds_ctx *c, int nsteps, float *total_ms, float *phase_ms)
 }
 
 ds_status ds_dust_density(ds_ctx *c) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c) return DS_ERR_ARG;
   ds_status st = finalize(c);
   if (st != DS_OK) return st;
@@ -1858,6 +1864,7 @@ ds_status ds_get_time(ds_ctx *c, int tube, double *Tm, double *dt_last, long lon
 
 ds_status ds_debug_cells(ds_ctx *c, int tube, int species, int *cell_key, int *head, int *next, int *ncand,
                          int *nnb, int *ncells) {
+  if (c && c->split) return fail(c, DS_ERR_STATE, "a split step is in progress (call ds_step_complete first)");
   if (!c) return DS_ERR_ARG;
   ds_status st = finalize(c);
   if (st != DS_OK) return st;

@@ -112,3 +112,42 @@ def test_fp32_slabs_track_one_domain(tmp_path):
     vscale = np.abs(g.vx).max()
     assert np.abs(got["0_vx"] - g.vx).mean() / vscale < 1e-4
     assert np.abs(got["1_vx"] - ref[1].vx).mean() / vscale < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_split_step_equals_one_step_and_refuses_calls_out_of_order(precision):
+    """ds_step_density + ds_step_complete with the CFL minimum read and written
+    back equal one ds_step bit for bit; calls out of order are refused with
+    DS_ERR_STATE and leave the step usable."""
+    from dustyshock3d_gb300 import ic
+    from dustyshock3d_gb300._lib import DsError
+    from dustyshock3d_gb300.solver import Solver
+    P, sp = ic.dusty_sod_tube(**TUBE)
+    P.precision = precision
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(2)
+        ref = [S.get_species(0, s) for s in range(2)], S.time(0)
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        with pytest.raises(DsError, match="DS_ERR_STATE"):
+            S.step_complete()
+        for _ in range(2):
+            S.step_density()
+            with pytest.raises(DsError, match="DS_ERR_STATE"):
+                S.step(1)
+            with pytest.raises(DsError, match="DS_ERR_STATE"):
+                S.step_density()
+            with pytest.raises(DsError, match="DS_ERR_STATE"):
+                S.set_tube(0, sp)
+            dtmin = S.cfl_min(0)
+            assert dtmin > 0
+            S.set_cfl_min(0, dtmin)
+            S.step_complete()
+        with pytest.raises(DsError, match="DS_ERR_STATE"):
+            S.set_cfl_min(0, 1.0)
+        got = [S.get_species(0, s) for s in range(2)], S.time(0)
+    assert got[1] == ref[1]
+    for s in range(2):
+        for f in FIELDS:
+            assert np.array_equal(getattr(got[0][s], f), getattr(ref[0][s], f)), (s, f)
