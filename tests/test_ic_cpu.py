@@ -135,6 +135,7 @@ def _nondefault_params():
     P.Gam_g, P.Speed_of_sound_gas, P.t_empty = 5.0 / 3.0, 0.9, 2e-3
     P.cell_w, P.idic_w, P.cfl = 0.031, 0.0125, 0.25
     P.n_dust, P.stencil, P.list_depth, P.force_list = 3, 2, 64, 320
+    P.list_skin, P.persistent, P.idic_lanes = 0.25, 1, 2
     P.mass_ratio, P.R_dust = [0.1, 1.0, 10.0], [0.0, 0.5, 2.0]
     P.t_stop_const, P.eps_empty = [1e-4, 1e-3, 1e-2], [0.1, 1.0, 10.0]
     P.precision = "fp32"

@@ -14,7 +14,7 @@ def test_parse_reference_style_init():
 
 
 def test_roundtrip_with_extensions():
-    P = Params(h=0.05, n_dust=1, mass_ratio=[2.0], precision="fp32")
+    P = Params(h=0.05, n_dust=1, mass_ratio=[2.0], precision="fp32", list_skin=0.2, persistent=1, idic_lanes=8)
     P.mode.periodic_y = True
     Q = parse_init_txt(write_init_txt(P))
     assert Q == P
