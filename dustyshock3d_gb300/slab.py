@@ -139,10 +139,11 @@ class TorchComm:
         counts = T.tensor([len(a) for a in send], dtype=T.int64, device=self.device)
         allc = [T.zeros(self.size, dtype=T.int64, device=self.device) for _ in range(self.size)]
         D.all_gather(allc, counts, group=self.group)
-        reqs, bufs = [], [None] * self.size
+        reqs, bufs, outgoing = [], [None] * self.size, []
         for r in range(self.size):
             if r != self.rank and len(send[r]):
                 t = T.from_numpy(np.ascontiguousarray(send[r], dtype=np.float64)).to(self.device)
+                outgoing.append(t)  # alive until every send has completed
                 reqs.append(D.isend(t, self._global(r), group=self.group))
         for r in range(self.size):
             n = int(allc[r][self.rank].item())
