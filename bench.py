@@ -19,10 +19,12 @@ Reported (one JSON line from rank 0):
              changed; separate_calls: ds_upload_* + ds_step + ds_download_*
   roofline   the gas density sweep (dominant kernel): compulsory bytes / duration
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on a bounded sample
+  reference_gpu the reference's own CUDA kernels (compiled unmodified into a
+             cubin where the reference tree exists) under a restatement of its
+             host loop, on its default run, beside the FP64 path on that run
 
 --impl reference times the reference algorithm on the host cores (the oracle,
-a CPU restatement of the reference's step; the reference's own GPU program
-cannot be built on the GPU host from this repository).
+a CPU restatement of the reference's step).
 """
 from __future__ import annotations
 
@@ -72,6 +74,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="default line: skip the 11.5M-particle tube record")
     ap.add_argument("--no-batch", action="store_true", help="default line: skip the 64-tube batch record")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="default line: skip the reference's own CUDA kernels on its default run")
     ap.add_argument("--t-end", type=float, default=0.2, help="accuracy_720k: end time of every run")
     ap.add_argument("--list-skin", type=float, default=0.0,
                     help="headline FP32 leg: reuse the recorded neighbour lists across steps with this skin "
@@ -213,6 +217,70 @@ def time_cpu_params(P, sp, steps, budget_s=25.0):
         el += time.perf_counter() - t0
         done += 1
     return n * done / el, f"{done} FP64 step(s) of the full {n}-particle tube from t=0 ({el:.1f} s)", n
+
+
+def reference_init_tube():
+    """The reference's own default run: ds_params_init (the values of its
+    Init.txt) and its generator init_Sod_X_Dust (323,584 gas + 2 x 323,584
+    dust), in reference mode."""
+    import ctypes
+
+    from dustyshock3d_gb300 import _lib, ic
+    L = _lib.load()
+    c = _lib.DsParams()
+    _lib.check(L, None, L.ds_params_init(ctypes.byref(c)), "ds_params_init")
+    return ic.init_sod_x_dust(_lib.params_from_c(c), before_first="skip")
+
+
+def reference_gpu_record(P=None, sp=None, steps=3):
+    """The reference's own CUDA kernels on this GPU against this library's FP64
+    path, on the reference's default run (both from t = 0, `steps` steps).
+
+    The reference's arm: kernel.cu and IDIC.h compiled unmodified into a cubin
+    (oracle/build_ref_gpu.sh, where the reference tree exists), launched by a
+    restatement of its host loop (oracle/ref_gpu.c): host cell lists, one
+    launch and one device synchronize per stencil offset, host IDIC solve,
+    blocking copies -- wall time per step, the median of steps 2.. (the first
+    pays first-launch costs).  This library's arm: the FP64 path (the same
+    operation order as the reference's host build), one untimed step, then
+    steps - 1 graph replays between CUDA events.  Both states are compared
+    after the same steps: the reference's kernels contract multiply-adds
+    (nvcc's default), so they differ from the FP64 path by rounding only."""
+    import numpy as np
+
+    from dustyshock3d_gb300.solver import Solver
+    from oracle import ref_gpu
+    why = ref_gpu.available()
+    if why:
+        return {"unavailable": why}
+    if P is None:
+        P, sp = reference_init_tube()
+    n = sum(q.n for q in sp)
+    steps = max(2, steps)
+    with Solver(P) as S:
+        S.set_tube(0, sp)
+        S.step(1)
+        ms = S.step_timed_graph(steps - 1)
+        ours = [S.get_species(0, s) for s in range(3)]
+    R = ref_gpu.RefGPU(P, sp).step(steps)
+    ref_s = float(np.median(R.step_s[1:]))
+    diff = {}
+    for s, tag in ((0, "gas"), (1, "dust1"), (2, "dust2")):
+        for f in ("x", "vx", "rho"):
+            a, b = getattr(R.species[s], f), getattr(ours[s], f)
+            diff[f"{tag}_{f}"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    ours_v = n * (steps - 1) / (ms * 1e-3)
+    return {"workload": "reference_init", "particles": n, "steps": steps,
+            "reference_kernels": {"value": n / ref_s, "unit": "particle-steps/s", "ms_per_step": 1e3 * ref_s,
+                                  "step_ms": [1e3 * t for t in R.step_s],
+                                  "what": "the reference's CUDA kernels (kernel.cu, IDIC.h compiled unmodified, "
+                                          "nvcc -O3, sm_103a) under a restatement of its host loop: host lists, "
+                                          "~120 launches each followed by a device synchronize, host IDIC, "
+                                          "blocking copies; wall time per step, median of steps 2.."},
+            "fp64_path": {"value": ours_v, "unit": "particle-steps/s", "ms_per_step": ms / (steps - 1),
+                          "what": "this library's FP64 path, CUDA events around steps - 1 graph replays"},
+            "fp64_path_over_reference_kernels": ours_v * ref_s / n,
+            "max_rel_diff_after_steps": diff}
 
 
 def batch64_tubes(seed):
@@ -609,6 +677,9 @@ def run_ours(args):
         bms = dist_max(dist, bms)
         batch["value"] = n_batch_all * 10 / (bms * 1e-3)  # whole job: all 64 tubes over the slowest rank
         batch["ms_per_step"] = bms / 10
+    ref_gpu_rec = None
+    if not args.no_ref_gpu and name == DEFAULT_WORKLOAD and rank == 0:
+        ref_gpu_rec = reference_gpu_record()
     clk = clocks.stop()
 
     if rank != 0:
@@ -644,7 +715,7 @@ def run_ours(args):
             "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
                                                                      phase)},
             "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "dusty_sod_5760k": c3, "batch64": batch,
+            "dusty_sod_5760k": c3, "batch64": batch, "reference_gpu": ref_gpu_rec,
             "gpu_launches": kps * args.steps, "clocks": clk}
     if args.list_skin > 0:
         line["list_reuse"] = {"skin_h": args.list_skin, "steps": list_steps, "steps_that_rebuilt": list_rebuilds}
@@ -852,21 +923,14 @@ def run_reference_init(args):
     (CUDA events around the step graphs) and end to end through
     ds_bind_host / ds_step_host; the CPU oracle on the host cores beside it.
     The run has 40 steps in all: --warmup steps, then up to --steps of the
-    rest are timed.  This is the like-for-like GPU number for the reference's
-    own CUDA program on the same input (which cannot be built on the GPU host)
-    and for its loops built for the host (timed where the reference tree
-    exists, oracle/compare_cpu_baselines.py)."""
-    import ctypes
-
-    from dustyshock3d_gb300 import _lib, ic
+    rest are timed.  Beside it, the reference's own CUDA kernels on the same
+    input and GPU (reference_gpu_record), and its loops built for the host
+    (timed where the reference tree exists, oracle/compare_cpu_baselines.py)."""
     from dustyshock3d_gb300.solver import Solver
     ws, rank, dist = dist_setup()
     if rank != 0:
         return 0
-    L = _lib.load()
-    c = _lib.DsParams()
-    _lib.check(L, None, L.ds_params_init(ctypes.byref(c)), "ds_params_init")
-    P, sp = ic.init_sod_x_dust(_lib.params_from_c(c), before_first="skip")
+    P, sp = reference_init_tube()
     n = sum(q.n for q in sp)
     total = int(round(P.T_end / P.tau))
     steps = max(1, min(args.steps, total - args.warmup))
@@ -879,6 +943,7 @@ def run_reference_init(args):
         kps = S.kernels_per_step()
     el, h2d, d2h = e2e_run(P, sp, steps, args.warmup, bound=True)
     clk = clocks.stop()
+    refk = None if args.no_ref_gpu else reference_gpu_record(P, sp)
     v, sample, _ = time_cpu_params(P, sp, 1)
     line = {"metric": "particle-steps/s", "value": n * steps / (ms * 1e-3), "unit": "particle-steps/s",
             "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
@@ -891,7 +956,7 @@ def run_reference_init(args):
                     "path": "ds_bind_host + ds_step_host(1) per step, fp64 path"},
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores(), "kind": "port",
                              "sample": sample},
-            "gpu_launches": kps * steps, "clocks": clk}
+            "reference_gpu": refk, "gpu_launches": kps * steps, "clocks": clk}
     print(json.dumps(line))
     return 0
 
