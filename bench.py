@@ -273,6 +273,7 @@ def reference_gpu_record(P=None, sp=None, steps=3):
     return {"workload": "reference_init", "particles": n, "steps": steps,
             "reference_kernels": {"value": n / ref_s, "unit": "particle-steps/s", "ms_per_step": 1e3 * ref_s,
                                   "step_ms": [1e3 * t for t in R.step_s],
+                                  "phase_ms_per_step": {k: 1e3 * v / steps for k, v in R.phase_s.items()},
                                   "what": "the reference's CUDA kernels (kernel.cu, IDIC.h compiled unmodified, "
                                           "nvcc -O3, sm_103a) under a restatement of its host loop: host lists, "
                                           "~120 launches each followed by a device synchronize, host IDIC, "

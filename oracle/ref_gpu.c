@@ -158,14 +158,42 @@ out:
   return -1;
 }
 
+static double now_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+/* Wall time of the last rg_run by kind of work: host cell lists, kernels
+ * (launch + synchronize), blocking copies, host IDIC averages and solve. */
+enum { PH_LISTS, PH_KERNELS, PH_COPIES, PH_IDIC, PH_N };
+static double g_phase[PH_N];
+
 /* ---- launches: the reference's gridSize / blockSize, then a synchronize ---- */
 static unsigned g_blocks;
 static int launch(int k, void **args, int sync) {
-  if (cu_check(D.LaunchKernel(g_fn[k], g_blocks, 1, 1, 16, 16, 1, 0, NULL, args, NULL), kname[k])) return -1;
-  return sync ? cu_check(D.CtxSynchronize(), "cudaDeviceSynchronize") : 0;
+  const double t = now_s();
+  int r = cu_check(D.LaunchKernel(g_fn[k], g_blocks, 1, 1, 16, 16, 1, 0, NULL, args, NULL), kname[k]);
+  if (!r && sync) r = cu_check(D.CtxSynchronize(), "cudaDeviceSynchronize");
+  g_phase[PH_KERNELS] += now_s() - t;
+  return r;
 }
-static int h2d(CUdeviceptr d, const void *h, size_t n) { return cu_check(D.MemcpyHtoD(d, h, n), "cudaMemcpy H2D"); }
-static int d2h(void *h, CUdeviceptr d, size_t n) { return cu_check(D.MemcpyDtoH(h, d, n), "cudaMemcpy D2H"); }
+static int h2d(CUdeviceptr d, const void *h, size_t n) {
+  const double t = now_s();
+  const int r = cu_check(D.MemcpyHtoD(d, h, n), "cudaMemcpy H2D");
+  g_phase[PH_COPIES] += now_s() - t;
+  return r;
+}
+static int d2h(void *h, CUdeviceptr d, size_t n) {
+  const double t = now_s();
+  const int r = cu_check(D.MemcpyDtoH(h, d, n), "cudaMemcpy D2H");
+  g_phase[PH_COPIES] += now_s() - t;
+  return r;
+}
+
+void rg_phase_seconds(double *out) {
+  for (int k = 0; k < PH_N; k++) out[k] = g_phase[k];
+}
 
 /* device copies of one species' fields (kernel.cu:1800-1865) */
 typedef struct {
@@ -181,12 +209,6 @@ typedef struct {
   double *xx[2], *xy[2], *xz[2], *xnx[2], *xny[2], *xnz[2];
   int *dcount[2];
 } idic_cells;
-
-static double now_s(void) {
-  struct timespec t;
-  clock_gettime(CLOCK_MONOTONIC, &t);
-  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
-}
 
 /* Host linked list of one species (kernel.cu:1937-1955). */
 static void build_list(const orc_species *s, int Pm, double Clx, double Cly, double Clz, double Clh, int Cnx,
@@ -315,13 +337,16 @@ int rg_run(const orc_params *P, orc_species *sp, int nsteps, double *Tm, double 
   }
 
   orc_species *gas = &sp[0];
+  for (int k = 0; k < PH_N; k++) g_phase[k] = 0.0;  /* the steps only, not the set-up above */
   for (int step = 0; step < nsteps; step++) {
     const double t0 = now_s();
     *Tm = *Tm + tau; /* kernel.cu:1931 */
 
     /* cell lists of the three species, then up (kernel.cu:1937-2005) */
+    double th = now_s();
     for (int s = 0; s < 3; s++)
       build_list(&sp[s], Pm, Clx, Cly, Clz, Clh, Cnx, Cny, Number_of_fihd_cells, Cell[s], Ne[s], Nn[s]);
+    g_phase[PH_LISTS] += now_s() - th;
     for (int s = 0; s < 3; s++) {
       if (h2d(ds[s].cell, Cell[s], fc) || h2d(ds[s].nn, Nn[s], ni)) goto out;
     }
@@ -361,6 +386,7 @@ int rg_run(const orc_params *P, orc_species *sp, int nsteps, double *Tm, double 
     if (d2h(sp[1].ts, ds[1].ts, nd) || d2h(sp[2].ts, ds[2].ts, nd)) goto out;
 
     /* IDIC cell averages on the host (kernel.cu:2060-2211) */
+    th = now_s();
     for (int i = 0; i <= Number_of_average_cell; i++) {
       C.vxg[i] = C.vyg[i] = C.vzg[i] = C.rhog[i] = C.eg[i] = 0.0;
       C.gcount[i] = 0;
@@ -426,6 +452,7 @@ int rg_run(const orc_params *P, orc_species *sp, int nsteps, double *Tm, double 
       for (int k = 0; k < 2; k++)
         C.epsc[k][i] = (C.gcount[i] > 0 && C.dcount[0][i] > 0) ? C.dcount[k][i] * mas_gas_dust[k] / C.gcount[i]
                                                                 : eps_empty[k];
+    g_phase[PH_IDIC] += now_s() - th;
 
     /* force and energy rate (kernel.cu:2229-2268) */
     {
@@ -453,6 +480,7 @@ int rg_run(const orc_params *P, orc_species *sp, int nsteps, double *Tm, double 
 
     /* cell means of the gas acceleration and the two-species implicit solve
      * (kernel.cu:2294-2437) */
+    th = now_s();
     for (int p = 0; p <= Pm; p++) {
       const int c = idic_index(gas, p, X_min, Y_min, Z_min, average_cell_width, Nax, Nay);
       C.psix[c] = C.psix[c] + gas->ax[p];
@@ -522,6 +550,8 @@ int rg_run(const orc_params *P, orc_species *sp, int nsteps, double *Tm, double 
       for (int a = 0; a < 3; a++) *v2[a] = *v2[a] / tmp1;
       for (int a = 0; a < 3; a++) *vg[a] = *vg[a] / tmp1;
     }
+
+    g_phase[PH_IDIC] += now_s() - th;
 
     /* relaxation on the device (kernel.cu:2453-2495) */
     if (h2d(dvxg, C.vxg, cd) || h2d(dvyg, C.vyg, cd) || h2d(dvzg, C.vzg, cd)) goto out;

@@ -25,6 +25,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(oracle.BUILD_DIR, "libref_gpu.so")
 CUBIN = os.path.join(HERE, "_ref", "ref_kernels.cubin")
 
+# rg_phase_seconds' order: host cell lists, kernels (launch + synchronize),
+# blocking copies, host IDIC averages and solve
+PHASES = ("host_lists", "kernels", "copies", "host_idic")
+
 _lock = threading.Lock()
 _lib = None
 
@@ -64,6 +68,8 @@ def lib():
             L.rg_run.restype = ctypes.c_int
             L.rg_last_error.argtypes = []
             L.rg_last_error.restype = ctypes.c_char_p
+            L.rg_phase_seconds.argtypes = [ctypes.POINTER(ctypes.c_double)]
+            L.rg_phase_seconds.restype = None
             _lib = L
     return _lib
 
@@ -85,6 +91,8 @@ class RefGPU:
         if L.rg_open(CUBIN.encode()) != 0:
             raise RuntimeError("reference kernels: " + L.rg_last_error().decode())
         self.step_s: list[float] = []
+        # wall time of the steps by kind of work, summed over step() calls
+        self.phase_s = {k: 0.0 for k in PHASES}
 
     @property
     def species(self):
@@ -106,4 +114,8 @@ class RefGPU:
             raise RuntimeError("reference kernels: " + L.rg_last_error().decode())
         self.state.Tm = Tm.value
         self.step_s.extend(float(t) for t in times)
+        ph = np.zeros(len(PHASES), dtype=np.float64)
+        L.rg_phase_seconds(ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        for k, v in zip(PHASES, ph):
+            self.phase_s[k] += float(v)
         return self

@@ -50,6 +50,7 @@ def test_reference_kernels_track_the_oracle(name, nsteps):
         for f in fields:
             _close(getattr(a, f), getattr(b, f), f"{name} species {s} {f}")
     assert len(R.step_s) == nsteps and min(R.step_s) > 0.0
+    assert R.phase_s["kernels"] > 0.0 and sum(R.phase_s.values()) <= sum(R.step_s)
 
 
 def test_reference_kernels_track_the_fp64_path():

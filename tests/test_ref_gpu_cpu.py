@@ -11,7 +11,7 @@ from oracle import oracle, ref_gpu
 
 def test_library_builds_and_exports():
     L = ctypes.CDLL(ref_gpu.build(force=True))
-    for name in ("rg_open", "rg_run", "rg_last_error"):
+    for name in ("rg_open", "rg_run", "rg_last_error", "rg_phase_seconds"):
         assert hasattr(L, name), name
 
 
