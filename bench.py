@@ -314,7 +314,7 @@ def batch64_record(seed, steps, warmup, shard=None):
     ps = []
     for P, _ in tubes:
         Q = tune.apply(P, choice.stencil, choice.cell_factor, choice.list_depth, choice.persistent,
-                       choice.idic_lanes)
+                       choice.idic_lanes, choice.list_skin)
         Q.precision = "fp32"
         ps.append(Q)
     n = sum(sizes[i] for i in idx)
@@ -330,8 +330,8 @@ def batch64_record(seed, steps, warmup, shard=None):
            "warmup": warmup, "tubes": len(tubes), "particles": n, "seed": seed,
            "initial_conditions": "generated on the device (ds_init_tube)",
            "autotuned": dataclasses.asdict(choice), "tuning_s": tune_s,
-           "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, persistent=p, idic_lanes=q, ms=d)
-                          for a, b, c, p, q, d in log],
+           "tuning_log": [dict(stencil=a, cell_factor=b, list_depth=c, persistent=p, idic_lanes=q, list_skin=k,
+                               ms=d) for a, b, c, p, q, k, d in log],
            "device_bytes": mem,
            "phase_ms_per_step": {k: v / steps for k, v in zip(("sort", "density", "force", "idic_update"), phase)},
            "gpu_launches": kps * steps}

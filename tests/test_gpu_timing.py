@@ -38,14 +38,27 @@ def test_autotuner_keeps_the_fastest_candidate():
     rng = np.random.default_rng(7)
     tubes = [ic.uneven_tube(**ic.draw_tube_params(rng, (2.0e4, 4.0e4))) for _ in range(2)]
     best, log = tune.tune(tubes, sample=2, warmup=1, steps=2,
-                          candidates=[(2, 1.001, 32), (1, 2.002, 32), (4, 0.5005, 32)])
-    timed = [row for row in log if row[5] is not None]
+                          candidates=[(2, 1.001, 32), (1, 2.002, 32), (4, 0.5005, 32)], skin_candidates=())
+    timed = [row for row in log if row[6] is not None]
     assert timed, log
-    assert best.ms_per_step == min(row[5] for row in timed)
+    assert best.ms_per_step == min(row[6] for row in timed)
+    assert best.list_skin == 0.0
     assert (best.stencil, best.cell_factor, best.persistent, best.idic_lanes) in \
         [(row[0], row[1], row[3], row[4]) for row in timed]
     # the launch shapes were tried for the winning grid
     assert {(row[3], row[4]) for row in timed} >= set(tune.LAUNCH_CANDIDATES)
+
+
+def test_autotuner_times_the_skins_for_the_winner():
+    rng = np.random.default_rng(11)
+    tubes = [ic.uneven_tube(**ic.draw_tube_params(rng, (2.0e4, 4.0e4))) for _ in range(2)]
+    best, log = tune.tune(tubes, sample=2, warmup=1, steps=2, candidates=[(2, 1.001, 32)],
+                          launch_candidates=[(0, 4)], skin_steps=6)
+    skin_rows = log[-(1 + len(tune.SKIN_CANDIDATES)):]
+    assert [row[5] for row in skin_rows] == [0.0] + list(tune.SKIN_CANDIDATES)
+    assert all(row[6] is not None for row in skin_rows)
+    fastest = min(skin_rows, key=lambda row: row[6])
+    assert (best.list_skin, best.ms_per_step) == (fastest[5], fastest[6])
 
 
 @pytest.mark.parametrize("persistent,lanes", [(1, 4), (0, 2), (1, 8)])
