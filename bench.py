@@ -52,6 +52,7 @@ WORKLOADS = {
     "dusty_sod_5760k": (1 / 1600, 0.05, "dusty Sod tube, 5.76M gas + 5.76M dust (left dx 1/1600, 0.05^2)"),
 }
 DEFAULT_WORKLOAD = "dusty_sod_720k"
+DEFAULT_SKIN = 0.15  # list reuse of the FP32 legs (units of h)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -77,9 +78,10 @@ def parse():
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="default line: skip the reference's own CUDA kernels on its default run")
     ap.add_argument("--t-end", type=float, default=0.2, help="accuracy_720k: end time of every run")
-    ap.add_argument("--list-skin", type=float, default=0.0,
-                    help="headline FP32 leg: reuse the recorded neighbour lists across steps with this skin "
-                         "(units of h; 0: off, the default: measured slower on this workload)")
+    ap.add_argument("--list-skin", type=float, default=DEFAULT_SKIN,
+                    help="FP32 legs of the default line: reuse the recorded neighbour lists across steps with this "
+                         "skin (units of h; 0: off).  0.15 measured fastest on the 720k tube, device-resident and "
+                         "end to end")
     return ap.parse_args()
 
 
@@ -338,9 +340,10 @@ def batch64_record(seed, steps, warmup, shard=None):
     return rec, sum(sizes), total_ms
 
 
-def device_tube_record(name, steps32=10, steps64=2, warmup=2):
-    """One tube generated on the device, timed on the FP32 and the FP64 path
-    (CUDA events around the step graphs, after warm-up steps)."""
+def device_tube_record(name, steps32=10, steps64=2, warmup=2, skin=0.0):
+    """One tube generated on the device, timed on the FP32 (list reuse with
+    `skin`) and the FP64 path (CUDA events around the step graphs, after
+    warm-up steps)."""
     from dustyshock3d_gb300 import ic
     from dustyshock3d_gb300.solver import Solver
     dx, Ly, desc = WORKLOADS[name]
@@ -351,12 +354,16 @@ def device_tube_record(name, steps32=10, steps64=2, warmup=2):
     for prec, steps, wu in (("fp32", steps32, warmup), ("fp64", steps64, 1)):
         Q = P.copy()
         Q.precision = prec
+        if prec == "fp32":
+            Q.list_skin = skin
         with Solver(Q) as S:
             S.init_tube(0, spec)
             S.step(wu)
             ms = S.step_timed_graph(steps)
             rec = {"value": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps, "warmup": wu}
             if prec == "fp32":
+                rec["list_skin_h"] = skin
+                rec["list_rebuilds_steps"] = list(S.list_stats(0))
                 _, phase = S.step_timed(steps)
                 rec["phase_ms_per_step"] = {k: v / steps for k, v in
                                             zip(("sort", "density", "force", "idic_update"), phase)}
@@ -492,14 +499,11 @@ def batch64_sizes(seed):
     return [sum(spec.plan()[1]) for _, spec in batch64_tubes(seed)]
 
 
-def force_bytes_per_particle(fp32: bool, hpp: bool) -> int:
-    """Compulsory bytes of one force-sweep launch per gas particle (each input
-    array read once, each output written once)."""
-    if fp32:
-        # pos32, vm32, hyd32 float4 (48) + x, y, z (24) + m, p, rho (24) + Ind (4); out ax, ay, az, edot (32)
-        return 48 + 24 + 24 + 4 + 32
-    # x, y, z, vx, vy, vz, m, rho, p-derived c and p/rho^2 (72) + h (8) + pos32 (16) + Ind (4); out 32
-    return 72 + (8 if hpp else 0) + 16 + 4 + 32
+# Compulsory bytes of one launch of the FP32 force sweep over the recorded
+# lists per gas particle, not counting the 4-byte entries: read pos32, vm32,
+# hyd32 (48), Ind and the entry count (8); write ax, ay, az and the energy
+# rate (32, FP64).
+FORCE_LIST_BYTES_PER_PARTICLE = 48 + 8 + 32
 
 
 def e2e_run(P, sp, steps, warmup, bound=True):
@@ -613,9 +617,14 @@ def run_ours(args):
     # one with events between phases), then the recorded force neighbours of
     # the final state (0 < r < 2 max(h_i, h_j), counted by the parity hook)
     _, phase = S.step_timed(args.steps)
+    list_rebuilds2, list_steps2 = S.list_stats(0)
     dbg = S.debug_cells(0, 0)
     free = S.get_species(0, 0).ind == 0
     list_entries = int(dbg["nnb"][free].sum())
+    # the entries the list kernels stream: the recorded lists (the particle
+    # itself and, with a skin, the partners in the skin's shell among them)
+    fcount, _ = S.debug_force_lists(0, cap=1)
+    streamed_entries = int(fcount[fcount > 0].sum())
     cand_per_pair = {"stencil_cells": float(dbg["ncand"][free].sum() / max(list_entries, 1)),
                      "note": "particles in the cells of each gas particle's stencil per recorded pair "
                              "(0 < r < 2 max(h_i, h_j)); the FP32 walk screens only the x window of each row, "
@@ -669,7 +678,7 @@ def run_ours(args):
     c3 = None
     if not args.no_c3 and name == DEFAULT_WORKLOAD:
         barrier(dist)
-        c3 = device_tube_record("dusty_sod_5760k")
+        c3 = device_tube_record("dusty_sod_5760k", skin=args.list_skin)
     batch = None
     if not args.no_batch and name == DEFAULT_WORKLOAD:
         barrier(dist)
@@ -687,19 +696,45 @@ def run_ours(args):
         return 0
     peak, peak_kind = peak_hbm()
     dens_ms = phase[1] / args.steps
-    alg = density_bytes_per_particle(P.mode.h_per_particle) * n_gas + 4 * list_entries
-    achieved = alg / (dens_ms * 1e-3) / 1e9
-    tr = profile_traffic(os.path.join(ROOT, "profiles", "density32_dusty_sod_720k.txt"))
-    roof = {"kernel": "k_density32 (gas density + EOS + force-list record, FP32)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "traffic": None if tr is None else tr * n_gas,
-            "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dens_ms,
-            "list_entries_per_launch": list_entries,
-            "note": "issue-bound, not HBM-bound: every particle screens the candidates of 27 (or 125) cells "
-                    "in FP32; traffic from the committed ncu capture of this workload"}
-    roof["issue"] = issue_ceiling(os.path.join(ROOT, "profiles", "density32_dusty_sod_720k.txt"), n_gas, dens_ms,
-                                  clk)
-    roof["candidates_per_pair"] = cand_per_pair
+    dens_prof = os.path.join(ROOT, "profiles", "density32_dusty_sod_720k.txt")
+    dens = {"kernel": "k_density32 (gas density + EOS + force-list record, FP32)",
+            "algorithmic_bytes_per_launch": density_bytes_per_particle(P.mode.h_per_particle) * n_gas
+            + 4 * list_entries, "list_entries_per_launch": list_entries, "candidates_per_pair": cand_per_pair}
+    if args.list_skin > 0:
+        # with list reuse the force sweep over the lists runs every step and
+        # takes the largest share; the density phase mixes the recording walk
+        # (steps that re-sort) and the streamed lists (steps that keep them)
+        f_ms = phase[2] / args.steps
+        prof = os.path.join(ROOT, "profiles", "force32_list_dusty_sod_720k_skin015.txt")
+        alg = FORCE_LIST_BYTES_PER_PARTICLE * n_gas + 4 * streamed_entries
+        achieved = alg / (f_ms * 1e-3) / 1e9
+        tr = profile_traffic(prof)
+        roof = {"kernel": "k_force32_list (force + energy rate over the recorded lists, FP32)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": None if tr is None else tr * n_gas,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": f_ms,
+                "list_entries_per_launch": streamed_entries,
+                "note": "launch time: the force phase (k_tstop and k_dt, ~0.01 ms, run in it; the overflow walk runs "
+                        "beside it on a second stream); algorithmic bytes: 88 per gas particle + 4 per streamed "
+                        "entry; traffic from the committed ncu capture of this workload"}
+        roof["issue"] = issue_ceiling(prof, n_gas, f_ms, clk)
+        dens["phase_ms_per_step"] = dens_ms
+        dens["note"] = ("with list reuse the density phase is the recording walk on steps that re-sort and the "
+                        "streamed lists (k_density32_lst) on the others")
+        roof["density_sweep"] = dens
+    else:
+        alg = dens["algorithmic_bytes_per_launch"]
+        achieved = alg / (dens_ms * 1e-3) / 1e9
+        tr = profile_traffic(dens_prof)
+        roof = {"kernel": dens["kernel"], "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": None if tr is None else tr * n_gas,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dens_ms,
+                "list_entries_per_launch": list_entries,
+                "note": "issue-bound, not HBM-bound: every particle screens the candidates of 27 (or 125) cells "
+                        "in FP32; traffic from the committed ncu capture of this workload"}
+        roof["issue"] = issue_ceiling(dens_prof, n_gas, dens_ms, clk)
+        roof["candidates_per_pair"] = cand_per_pair
     cpu = None
     if not args.no_cpu_baseline:
         v, sample, _ = time_cpu(name, 3)
@@ -719,7 +754,9 @@ def run_ours(args):
             "dusty_sod_5760k": c3, "batch64": batch, "reference_gpu": ref_gpu_rec,
             "gpu_launches": kps * args.steps, "clocks": clk}
     if args.list_skin > 0:
-        line["list_reuse"] = {"skin_h": args.list_skin, "steps": list_steps, "steps_that_rebuilt": list_rebuilds}
+        line["list_reuse"] = {"skin_h": args.list_skin, "steps": list_steps, "steps_that_rebuilt": list_rebuilds,
+                              "phase_pass": {"steps": list_steps2 - list_steps,
+                                             "steps_that_rebuilt": list_rebuilds2 - list_rebuilds}}
     print(json.dumps(line))
     return 0
 

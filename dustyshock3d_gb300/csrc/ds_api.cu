@@ -426,8 +426,12 @@ const uint32_t *fast_skey(const ds_ctx *c) {
 // on the FP32 path (the parity hook's lists).  reuse: the step's list-reuse
 // decisions apply (TubeState::rebuild, set by the start-of-step test); any
 // other sort of a list-reuse context re-orders every tube, so the next step
-// must re-sort and record (the force flag).
-void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorder = nullptr, bool reuse = false) {
+// must re-sort and record (the force flag).  slot_pid (FP32 path, a step on
+// bound host arrays with list reuse): the current buffer holds the host's
+// state in caller order and slot i of the previous order held particle
+// slot_pid[i]; the sort starts from the previous order, as a resident step's.
+void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorder = nullptr, bool reuse = false,
+                  const int *slot_pid = nullptr) {
   cudaStream_t s = c->stream;
   DevState src = c->buf[c->parity].view();
   DevState dst = c->buf[c->parity ^ 1].view();
@@ -437,8 +441,9 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorde
   const TubeState *rts = ru ? c->d_tstate : nullptr;
   const int *run_if = ru ? c->d_any : nullptr;
   c->last_xl = xl;
+  const int *sp = (ru && slot_pid) ? slot_pid : nullptr;
   ds_launch_keys(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), src, c->kin, c->vin, fast, s, rts,
-                 ru ? fast_skey(c) : nullptr);
+                 ru ? fast_skey(c) : nullptr, sp);
   bool alt = false;
   ds_radix_sort(c->kin, c->vin, c->kalt, c->valt, c->N, c->key_bits + xl, c->rs_scratch, s, &alt, run_if);
   const uint32_t *skey = alt ? c->kalt : c->kin;
@@ -446,7 +451,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorde
   if (before_reorder) cudaStreamWaitEvent(s, before_reorder, 0);  // fields still arriving from the host
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
                     c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, c->d_flags, fast, s, rts,
-                    (c->reuse && fast) ? c->pos_ref : nullptr);
+                    (c->reuse && fast) ? c->pos_ref : nullptr, sp);
   ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s, run_if);
   c->skey = skey;
   if (c->any_stencil2)
@@ -560,11 +565,16 @@ __global__ void k_inverse(const Chunk *chunks, const TubeDesc *tubes, const int 
 // Into the other buffer set in caller order (slot seg_begin + p = particle p):
 // bound fields from the host, unbound ones gathered from the resident state;
 // segments without host arrays carried over slot for slot.  PART 0: x, y, z
-// and pid (what the cell keys read); PART 1: the other fields and Ind.
-template <int PART>
+// and pid (what the cell keys read), and with EARLY also h and Ind (what the
+// list-reuse test reads); PART 1: the other fields.
+template <bool EARLY>
+__host__ __device__ constexpr int bound_part(int f) {
+  return (f == FX || f == FY || f == FZ || (EARLY && f == FH)) ? 0 : 1;
+}
+template <int PART, bool EARLY>
 __device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *tubes, const BoundSeg *bs,
                                                const int *inv, DevState src, DevState dst) {
-  constexpr int F0 = PART == 0 ? 0 : 3, F1 = PART == 0 ? 3 : NF;
+  constexpr bool IND = (PART == 0) == EARLY;  // Ind travels in this part
   const int i = ch.begin + (int)threadIdx.x;
   if (i >= ch.end) return;
   const BoundSeg &B = bs[ch.tube * DS_MAXS + ch.species];
@@ -574,27 +584,31 @@ __device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *
                     dst.rho, dst.p, dst.e, dst.m, dst.h, dst.ts};
   if (!B.bound) {
 #pragma unroll
-    for (int f = F0; f < F1; f++) df[f][i] = sf[f][i];
+    for (int f = 0; f < NF; f++)
+      if (bound_part<EARLY>(f) == PART) df[f][i] = sf[f][i];
     if (PART == 0) dst.pid[i] = src.pid[i];
-    else dst.ind[i] = src.ind[i];
+    if (IND) dst.ind[i] = src.ind[i];
     return;
   }
   const int p = i - tubes[ch.tube].seg_begin[ch.species];
   const int q = inv[i];  // the resident slot of particle p
-  double v[F1 - F0];     // every load before any store: the link's latency is paid once
+  double v[NF];          // every load before any store: the link's latency is paid once
 #pragma unroll
-  for (int f = F0; f < F1; f++) v[f - F0] = B.f[f] ? B.f[f][p] : sf[f][q];
+  for (int f = 0; f < NF; f++)
+    if (bound_part<EARLY>(f) == PART) v[f] = B.f[f] ? B.f[f][p] : sf[f][q];
   int k = 0;
-  if (PART == 1) k = B.ind ? B.ind[p] : src.ind[q];
+  if (IND) k = B.ind ? B.ind[p] : src.ind[q];
 #pragma unroll
-  for (int f = F0; f < F1; f++) df[f][i] = v[f - F0];
+  for (int f = 0; f < NF; f++)
+    if (bound_part<EARLY>(f) == PART) df[f][i] = v[f];
   if (PART == 0) dst.pid[i] = p;
-  else dst.ind[i] = k;
+  if (IND) dst.ind[i] = k;
 }
-template <int PART>
+template <int PART, bool EARLY>
 __global__ void k_bound_in(const Chunk *chunks, int nchunks, const TubeDesc *tubes, const BoundSeg *bs,
                            const int *inv, DevState src, DevState dst) {
-  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) bound_in_chunk<PART>(chunks[c], tubes, bs, inv, src, dst);
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
+    bound_in_chunk<PART, EARLY>(chunks[c], tubes, bs, inv, src, dst);
 }
 
 // The bound fields a step has made final, back to the host in caller order:
@@ -645,13 +659,31 @@ void enqueue_bound_step(ds_ctx *c) {
   // loads in flight, and a grid of every chunk would take all the SMs' slots
   // from the sort and the sweeps they are meant to overlap.
   const int nside = nch < c->side_blocks ? nch : c->side_blocks;
-  k_bound_in<0><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
-  k_bound_in<1><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+  // with list reuse the start-of-step test reads h and Ind too: they come
+  // with the positions, on the first stream
+  const bool ru = c->reuse && c->any_fp32;
+  if (ru) {
+    k_bound_in<0, true><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+    k_bound_in<1, true><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+  } else {
+    k_bound_in<0, false><<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+    k_bound_in<1, false><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, old, neu);
+  }
   cudaEventRecord(c->e_up, s2);
   c->parity = P0 ^ 1;  // the caller-order state; the sort brings it back to P0
   ds_launch_step_begin(c->d_tubes, c->d_tstate, c->ntubes, c->d_work, s);
-  enqueue_sort(c, false, c->e_up);  // the host's arrays: every tube re-sorts
-  if (c->reuse) ds_launch_list_decide(c->d_tubes, c->d_tstate, c->ntubes, c->d_force, c->d_any, s);
+  if (ru) {
+    // List reuse: the test measures the host's positions against the recorded
+    // ones slot by slot (slot q of the resident order holds particle
+    // old.pid[q]); a tube that keeps its lists keeps its slot order, and one
+    // that re-sorts starts from it, as a step on the resident state does.
+    ds_launch_list_test(c->d_tubes, c->d_tstate, c->ntubes, c->d_ch_gas, (int)c->ch_gas.size(), neu, fast_skey(c),
+                        c->pos_ref, c->disp, c->d_nseg_key0, c->d_nseg_tube, c->d_nseg_species, c->nnseg, c->nkeys,
+                        c->cell_start, c->xl, c->krad, c->cellstat, c->d_force, c->d_any, s, old.pid, old);
+    enqueue_sort(c, false, c->e_up, true, old.pid);
+  } else {
+    enqueue_sort(c, false, c->e_up);  // the host's arrays: every tube re-sorts
+  }
   k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->buf[c->parity].pid, c->inv);
   enqueue_physics(c, nullptr, c->e_dens, c->e_force);
   DevState st = c->buf[c->parity].view();

@@ -68,30 +68,37 @@ __device__ __forceinline__ int fast_idic_cell(const TubeDesc &T, double x, doubl
 // keeps its slot order.  Its slots get the keys of the last sort (prev, the
 // sort's output of the previous step, slot by slot) with their own slot as the
 // value, so the stable sort leaves them where they are.
+//
+// slot_pid (FP32 path, a step on bound host arrays with list reuse): st holds
+// the host's state in caller order, and slot i of the previous order holds
+// particle slot_pid[i].  Slot i then keys that particle (st at seg_begin +
+// slot_pid[i], which is also the value), so cells keep the previous slot
+// order exactly as a step on the resident state does.
 template <bool FAST>
 __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                       uint32_t *vin, const TubeState *ts, const uint32_t *prev) {
+                       uint32_t *vin, const TubeState *ts, const uint32_t *prev, const int *slot_pid) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int i = ch.begin + threadIdx.x;
     if (i >= ch.end) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    const int j = (FAST && slot_pid) ? T.seg_begin[ch.species] + slot_pid[i] : i;  // the particle of slot i
     if (FAST && ts && !ts[ch.tube].rebuild) {
       kin[i] = prev[i];
-      vin[i] = (uint32_t)i;
+      vin[i] = (uint32_t)j;
       continue;
     }
-    const TubeDesc &T = tubes[ch.tube];
     int local;
     uint32_t bin = 0;
     if (FAST && (T.mode & M_GRID_PROPER)) {
       int ix, iy, iz;
-      ds_fast_proper_cell(T, st.x[i], st.y[i], st.z[i], ix, iy, iz);
+      ds_fast_proper_cell(T, st.x[j], st.y[j], st.z[j], ix, iy, iz);
       const bool in = ix >= 0 && ix < T.nx && iy >= 0 && iy < T.ny && iz >= 0 && iz < T.nz;
       local = in ? ix + iy * T.sy + iz * T.sz : T.ncells + 1;
       // FP32 path: the particle's x within its cell in 2^xl bins, below the
       // cell in the key, so that each cell -- and so each row of cells -- is
       // sorted by x (the low bits of the fine x index)
-      if (in) bin = (uint32_t)ds_fast_fine_x(T, st.x[i]) & ((1u << T.xl) - 1u);
+      if (in) bin = (uint32_t)ds_fast_fine_x(T, st.x[j]) & ((1u << T.xl) - 1u);
     } else {
       const int key = ds_raw_key(T, st.x[i], st.y[i], st.z[i]);
       if (!(T.mode & M_GRID_PROPER))
@@ -102,7 +109,7 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
     const int dst = FAST ? i : T.seg_begin[ch.species] + st.pid[i];
     kin[dst] = FAST ? ((uint32_t)(T.key_base[ch.species] + local) << T.xl) | bin
                     : (uint32_t)(T.key_base[ch.species] + local);
-    vin[dst] = (uint32_t)i;
+    vin[dst] = (uint32_t)j;
   }
 }
 
@@ -120,14 +127,16 @@ template <bool FAST>
 __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                           const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32,
                           int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid,
-                          int *flags, const TubeState *ts, float4 *pos_ref) {
+                          int *flags, const TubeState *ts, float4 *pos_ref, const int *slot_pid) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int q = ch.begin + threadIdx.x;
     if (q >= ch.end) continue;
     const TubeDesc &T = tubes[ch.tube];
     const bool keep = FAST && ts && !ts[ch.tube].rebuild;
-    const int j = keep ? q : (int)order[q];
+    // a kept tube's slot q holds the particle it held (k_keys): in src at q,
+    // or, from bound host arrays in caller order, at seg_begin + slot_pid[q]
+    const int j = keep ? (slot_pid ? T.seg_begin[ch.species] + slot_pid[q] : q) : (int)order[q];
     const double x = src.x[j], y = src.y[j], z = src.z[j];
     dst.x[q] = x; dst.y[q] = y; dst.z[q] = z;
     const double vx = src.vx[j], vy = src.vy[j], vz = src.vz[j];
@@ -887,8 +896,15 @@ __device__ __forceinline__ float4 list_offset(const TubeDesc &T, int ix, int iy,
 
 // displacement of every gas slot of a reusing tube since its lists were
 // recorded; a slot outside the grid marks its tube (re-sort)
+//
+// slot_pid (a step on bound host arrays): st holds the host's state in caller
+// order and slot q of the recorded order holds particle slot_pid[q]; res is the
+// resident state the lists were recorded on (slot order).  A particle whose h
+// or Ind the host has changed makes its tube re-sort: the lists' cut-offs and
+// membership assume both.
 __global__ void k_list_disp(const TubeDesc *tubes, TubeState *ts, const Chunk *chunks, int nchunks, DevState st,
-                            const uint32_t *skey, const float4 *pos_ref, float4 *disp, const int *force) {
+                            const uint32_t *skey, const float4 *pos_ref, float4 *disp, const int *force,
+                            const int *slot_pid, DevState res) {
   if (*force) return;
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
@@ -896,11 +912,14 @@ __global__ void k_list_disp(const TubeDesc *tubes, TubeState *ts, const Chunk *c
     if (q >= ch.end) continue;
     const TubeDesc &T = tubes[ch.tube];
     if (!(T.skin > 0.0) || !ts[ch.tube].built) continue;
+    const int j = slot_pid ? T.seg_begin[ch.species] + slot_pid[q] : q;
+    if (slot_pid && (dbl_bits(st.h[j]) != dbl_bits(res.h[q]) || st.ind[j] != res.ind[q]))
+      atomicMax(&ts[ch.tube].disp_bits, 0x7f800000u);  // +inf: re-sort
     const int local = (int)(skey[q] >> T.xl) - T.key_base[ch.species];
     float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
     if (local >= 0 && local < T.ncells) {
       const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
-      const float4 o = list_offset(T, ix, iy, iz, st.x[q], st.y[q], st.z[q]);
+      const float4 o = list_offset(T, ix, iy, iz, st.x[j], st.y[j], st.z[j]);
       const float4 r = pos_ref[q];
       d = make_float4(o.x - r.x, o.y - r.y, o.z - r.z, 0.0f);
     } else {
@@ -1113,24 +1132,27 @@ void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, int 
   k_step_begin<<<blocks_for(n, 64), 64, 0, s>>>(tubes, ts, ntubes, work);
 }
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
-                    uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts, const uint32_t *prev_skey) {
+                    uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts, const uint32_t *prev_skey,
+                    const int *slot_pid) {
   if (!nchunks) return;
-  if (fast) k_keys<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, reuse_ts, prev_skey);
-  else k_keys<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, nullptr, nullptr);
+  if (fast)
+    k_keys<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, reuse_ts, prev_skey, slot_pid);
+  else
+    k_keys<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, st, kin, vin, nullptr, nullptr, nullptr);
 }
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
-                       cudaStream_t s, const TubeState *reuse_ts, float4 *pos_ref) {
+                       cudaStream_t s, const TubeState *reuse_ts, float4 *pos_ref, const int *slot_pid) {
   if (!nchunks) return;
   if (fast)
     k_reorder<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, reuse_ts,
-                                                 pos_ref);
+                                                 pos_ref, slot_pid);
   else
     k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
                                                   idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, nullptr,
-                                                  nullptr);
+                                                  nullptr, nullptr);
 }
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if) {
@@ -1140,9 +1162,10 @@ void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const
                          int ngas_chunks, DevState st, const uint32_t *skey, const float4 *pos_ref, float4 *disp,
                          const int *nseg_key0, const int *nseg_tube, const int *nseg_species, int nseg, int nkeys,
                          const int *cell_start, int xl, const unsigned char *krad, float4 *cellstat, int *force,
-                         int *any, cudaStream_t s) {
+                         int *any, cudaStream_t s, const int *slot_pid, DevState res) {
   if (ngas_chunks)
-    k_list_disp<<<ngas_chunks, DS_CHUNK, 0, s>>>(tubes, ts, gas_chunks, ngas_chunks, st, skey, pos_ref, disp, force);
+    k_list_disp<<<ngas_chunks, DS_CHUNK, 0, s>>>(tubes, ts, gas_chunks, ngas_chunks, st, skey, pos_ref, disp, force,
+                                                 slot_pid, res);
   if (nkeys > 0) {
     const int b = blocks_for(nkeys, 128);
     k_list_cellstat<<<b, 128, 0, s>>>(tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, cell_start, xl,

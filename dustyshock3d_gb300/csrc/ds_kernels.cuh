@@ -30,21 +30,25 @@ void ds_launch_step_begin(const TubeDesc *tubes, TubeState *ts, int ntubes, int 
 // it slot for slot.  pos_ref receives the FP32 offsets of re-sorted tubes.
 void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, DevState st, uint32_t *kin,
                     uint32_t *vin, bool fast, cudaStream_t s, const TubeState *reuse_ts = nullptr,
-                    const uint32_t *prev_skey = nullptr);
+                    const uint32_t *prev_skey = nullptr, const int *slot_pid = nullptr);
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
-                       cudaStream_t s, const TubeState *reuse_ts = nullptr, float4 *pos_ref = nullptr);
+                       cudaStream_t s, const TubeState *reuse_ts = nullptr, float4 *pos_ref = nullptr,
+                       const int *slot_pid = nullptr);
 // run_if: skipped when *run_if == 0 (no tube re-sorted this step)
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if = nullptr);
 // List reuse: the start-of-step test (displacements, per-cell statistics, the
 // bound per tube) and the per-tube decision; *any = some tube re-sorts.
+// slot_pid / res (a step on bound host arrays): st is the host's state in
+// caller order, slot q of the recorded order holds particle slot_pid[q], res
+// is the resident state the lists were recorded on.
 void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const Chunk *gas_chunks,
                          int ngas_chunks, DevState st, const uint32_t *skey, const float4 *pos_ref, float4 *disp,
                          const int *nseg_key0, const int *nseg_tube, const int *nseg_species, int nseg, int nkeys,
                          const int *cell_start, int xl, const unsigned char *krad, float4 *cellstat, int *force,
-                         int *any, cudaStream_t s);
+                         int *any, cudaStream_t s, const int *slot_pid = nullptr, DevState res = DevState{});
 // split step: density and pressure of listed gas particles (caller indices idx;
 // val = rho[0..n) then p[0..n)), with the force sweep's per-particle inputs
 void ds_launch_set_hydro(const TubeDesc *tubes, int tube, int n, const int *idx, const double *val, const int *inv,

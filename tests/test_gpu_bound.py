@@ -150,3 +150,71 @@ def test_bind_errors():
         ptrs = (ctypes.POINTER(ctypes.c_double) * 15)()
         assert L.ds_bind_host(S.ctx, 0, 0, sp[0].n + 1, ptrs, None) == 1  # wrong count
         assert L.ds_bind_host(S.ctx, 0, 5, sp[0].n, ptrs, None) == 1      # no such species
+
+
+def _reuse_tube(skin):
+    """A cross-section that holds the periodic stencil of cells widened by the skin."""
+    P, sp = ic.dusty_sod_tube(dx_left=1 / 64, Ly=0.375, x_range=(-0.25, 0.25))
+    P.precision = "fp32"
+    P.list_skin = skin
+    return P, [s.copy().fill_missing() for s in sp]
+
+
+def test_bound_steps_with_list_reuse_equal_resident_steps():
+    """With list reuse a bound step keeps the recorded lists and the slot order
+    when the host's positions allow it, and re-sorts from the previous slot
+    order otherwise, exactly as a step on the resident state: bound steps on
+    unedited host arrays equal resident steps bit for bit, with the same
+    rebuild decisions."""
+    P, sp = _reuse_tube(0.15)
+    with Solver(P) as A, Solver(P) as B:
+        A.set_tube(0, sp)
+        B.set_tube(0, sp)
+        bound = _bind(B, _host_state(sp))
+        for step in range(10):
+            A.step(1)
+            B.step_host(1)
+            for k in range(2):
+                got = A.get_species(0, k)
+                for f in (GAS_OUT if k == 0 else DUST_OUT):
+                    assert np.array_equal(bound[k][0][f], getattr(got, f)), f"step {step + 1} species {k} {f}"
+        ra, na = A.list_stats(0)
+        rb, nb = B.list_stats(0)
+        assert (ra, na) == (rb, nb) and na == 10
+        assert 1 <= rb < nb, (rb, nb)  # some steps kept their lists
+        assert A.time() == B.time()
+
+
+@pytest.mark.parametrize("field", ["h", "ind"])
+def test_host_edit_of_h_or_ind_forces_a_rebuild(field):
+    """The lists' cut-offs and membership assume each particle's h and Ind: a
+    bound step whose host arrays changed either re-sorts and records, and its
+    results stay within the FP32 path's bounds of the plain upload cycle."""
+    P, sp = _reuse_tube(0.45)
+    ref = _host_state(sp)
+    with Solver(P) as A, Solver(P) as B:
+        A.set_tube(0, sp)
+        B.set_tube(0, sp)
+        bound = _bind(A, _host_state(sp))
+        for _ in range(3):
+            A.step_host(1)
+            _plain_step(B, ref)
+        r0, n0 = A.list_stats(0)
+        A.step_host(1)
+        _plain_step(B, ref)
+        r1, n1 = A.list_stats(0)
+        assert n1 == n0 + 1 and r1 == r0, "the lists should be kept on an unedited step"
+        i = int(np.nonzero(ref[0]["ind"] == 0)[0][len(ref[0]["ind"]) // 2])
+        if field == "h":
+            bound[0][0]["h"][i] *= 1.0 + 2.0 ** -40
+            ref[0]["h"][i] *= 1.0 + 2.0 ** -40
+        else:
+            bound[0][1][i] = 1
+            ref[0]["ind"][i] = 1
+        A.step_host(1)
+        _plain_step(B, ref)
+        r2, n2 = A.list_stats(0)
+        assert n2 == n1 + 1 and r2 == r1 + 1, "the edit should force a rebuild"
+        for f in ("x", "vx", "rho", "e"):
+            a, b = bound[0][0][f], ref[0][f]
+            assert np.abs(a - b).sum() <= 1e-5 * np.abs(b).sum() + 1e-30, f
