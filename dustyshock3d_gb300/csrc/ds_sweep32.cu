@@ -393,8 +393,11 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 #ifndef DS_FPIECE
 #define DS_FPIECE 2  // list entries per pipeline stage (measured: 2 beats 4)
 #endif
+#ifndef DS_FLIST_MINB
+#define DS_FLIST_MINB 7  // blocks per SM the force list kernel is built for (measured: 7 beats 6 and 8)
+#endif
 template <bool HPP>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
+__global__ void __launch_bounds__(DS_SWEEP_THREADS, DS_FLIST_MINB) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
   __shared__ int claim;
