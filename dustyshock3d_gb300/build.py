@@ -3,7 +3,9 @@
 nvcc, one -gencode (sm_103a), translation units compiled in parallel.  The FP64
 kernels that must follow the reference's operation order (ds_cells.cu,
 ds_sweep64.cu) are compiled with -fmad=false so nvcc does not contract a*b+c
-into FMAs; the initial-condition generator (ds_ic.cu) also keeps the host
+into FMAs; so are the FP32 sweeps (ds_sweep32.cu), whose multiply-adds are
+written out, so that a pair's bits do not depend on the kernel that
+evaluates it; the initial-condition generator (ds_ic.cu) also keeps the host
 compiler from contracting its plan arithmetic.
 """
 from __future__ import annotations
@@ -23,7 +25,7 @@ SOURCES = {
     "ds_sort.cu": [],
     "ds_cells.cu": ["-fmad=false"],
     "ds_sweep64.cu": ["-fmad=false"],
-    "ds_sweep32.cu": [],
+    "ds_sweep32.cu": ["-fmad=false"],
     "ds_ic.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "ds_inittxt.cu": [],
 }

@@ -27,22 +27,30 @@ struct Kahan {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-// M4 shape without normalisation, q = r/h >= 0 (kernel.cu:18-20)
+// This file is compiled without multiply-add contraction (-fmad=false): every
+// fused multiply-add below is written out (__fmaf_rn), so that the same pair
+// gives the same bits in every kernel that evaluates it (the recording walk and
+// the streamed lists, the force walk and the force lists), whatever registers
+// and schedule each kernel gets.
+
+// M4 shape without normalisation, q = r/h >= 0 (kernel.cu:18-20):
+// 1 - 1.5 q^2 + 0.75 q^3 = 1 + q^2 (0.75 q - 1.5), and 0.25 (2 - q)^3
 __device__ __forceinline__ float w_shape(float q) {
-  if (q < 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
+  if (q < 1.0f) return __fmaf_rn(q * q, __fmaf_rn(0.75f, q, -1.5f), 1.0f);
   if (q <= 2.0f) {
     const float t = 2.0f - q;
-    return 0.25f * t * t * t;
+    return (0.25f * t) * (t * t);
   }
   return 0.0f;
 }
 
-// derivative shape, q >= 0 (kernel.cu:34-36)
+// derivative shape, q >= 0 (kernel.cu:34-36): -3 q + 2.25 q^2 = q (2.25 q - 3),
+// and -0.75 (2 - q)^2
 __device__ __forceinline__ float dw_shape(float q) {
-  if (q <= 1.0f) return -3.0f * q + 2.25f * q * q;
+  if (q <= 1.0f) return q * __fmaf_rn(2.25f, q, -3.0f);
   if (q <= 2.0f) {
     const float t = 2.0f - q;
-    return -0.75f * t * t;
+    return -0.75f * (t * t);
   }
   return 0.0f;
 }
@@ -327,21 +335,21 @@ struct ForceSum {
     const float inv_d = rsqrtf(r2);
     const float dist = r2 * inv_d;
     const float hh = HPP ? 0.5f * (hi + pj.w) : hi;
-    const float nu = (vmi.x - vmj.x) * (-dx) + (vmi.y - vmj.y) * (-dy) + (vmi.z - vmj.z) * (-dz);
+    const float nu = __fmaf_rn(vmi.z - vmj.z, -dz, __fmaf_rn(vmi.y - vmj.y, -dy, (vmi.x - vmj.x) * (-dx)));
     float F = 0.0f;
     if (nu < 0.0f) {
       const float Cnu = 0.5f * (csi + hyj.x);
-      const float mu = __fdividef(hh * nu, r2 + eps * hh * hh);
-      F = __fdividef(-alpha * Cnu * mu + beta * mu * mu, 0.5f * (rhoi + hyj.z));
+      const float mu = __fdividef(hh * nu, __fmaf_rn(eps * hh, hh, r2));
+      F = __fdividef(__fmaf_rn(beta * mu, mu, (-alpha * Cnu) * mu), 0.5f * (rhoi + hyj.z));
     }
     float dWr = ni * dw_shape(dist * inv_hi);
     if (HPP) {
       const float inv_hj = hyj.w;
       const float nj = (float)(1.0 / 3.14159265) * inv_hj * inv_hj * inv_hj * inv_hj;
-      dWr = 0.5f * (dWr + nj * dw_shape(dist * inv_hj));
+      dWr = 0.5f * __fmaf_rn(nj, dw_shape(dist * inv_hj), dWr);
     }
     const float gd = dWr * inv_d;
-    et.add((mpi + mi * F * 0.5f) * nu * gd);
+    et.add((__fmaf_rn(mi * F, 0.5f, mpi) * nu) * gd);
     const float A = vmj.w * (pti + hyj.y + F) * gd;
     Ax.add(dx * A);
     Ay.add(dy * A);
