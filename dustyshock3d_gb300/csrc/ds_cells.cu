@@ -988,12 +988,29 @@ __device__ __forceinline__ int wrap_index(int c, int n) {
 // per gas cell c of a reusing tube: the largest dev_c + dev_c' + |m_c - m_c'|
 // over the non-empty cells c' within r_c + 1 cells (each unordered pair once:
 // c' after c in the (z, y, x) order of the offsets), max-reduced per tube into
-// disp_bits (a float >= 0 as bits; not finite -> +inf)
-__global__ void k_list_bound(const TubeDesc *tubes, TubeState *ts, const int *nseg_key0, const int *nseg_tube,
-                             const int *nseg_species, int nseg, int nkeys, const unsigned char *krad,
-                             const float4 *stat, const int *force) {
+// disp_bits (a float >= 0 as bits; not finite -> +inf).  One warp per cell,
+// its lanes over the offsets (the offsets after (0, 0, 0) in that order are
+// the cube indices after its centre); the block's warps combine their maxima
+// in shared memory for the tube of the block's first cell, so that the tube's
+// one address takes one atomic per block, not one per cell.
+#define DS_BOUND_WARPS 16
+__global__ void __launch_bounds__(32 * DS_BOUND_WARPS)
+    k_list_bound(const TubeDesc *tubes, TubeState *ts, const int *nseg_key0, const int *nseg_tube,
+                 const int *nseg_species, int nseg, int nkeys, const unsigned char *krad, const float4 *stat,
+                 const int *force) {
   if (*force) return;  // uniform over the grid
-  const int key = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned FULL = 0xffffffffu;
+  __shared__ unsigned s_acc;
+  __shared__ int s_tube, s_any;
+  const int lane = (int)(threadIdx.x & 31);
+  const int kfirst = (int)blockIdx.x * DS_BOUND_WARPS;
+  const int key = kfirst + (int)(threadIdx.x >> 5);  // one per warp
+  if (threadIdx.x == 0) {
+    s_acc = 0u;
+    s_any = 0;
+    s_tube = nseg_tube[find_seg(nseg_key0, nseg, kfirst < nkeys ? kfirst : nkeys - 1)];
+  }
+  __syncthreads();
   bool act = key < nkeys;
   int t = 0;
   if (act) {
@@ -1004,7 +1021,7 @@ __global__ void k_list_bound(const TubeDesc *tubes, TubeState *ts, const int *ns
   float m = 0.0f;
   bool bad = false;
   const float4 a = act ? stat[key] : make_float4(0.f, 0.f, 0.f, -1.f);
-  act = act && a.w >= 0.0f;
+  act = act && a.w >= 0.0f;  // uniform over the warp
   if (act) {
     const TubeDesc &T = tubes[t];
     const int kb = T.key_base[0];
@@ -1012,30 +1029,52 @@ __global__ void k_list_bound(const TubeDesc *tubes, TubeState *ts, const int *ns
     const int ix = local % T.nx, iy = (local / T.nx) % T.ny, iz = local / (T.nx * T.ny);
     int r = T.stencil == 1 ? 1 : (int)krad[key];
     r = (r < 1 ? 1 : (r > T.stencil ? T.stencil : r)) + 1;
-    m = 2.0f * a.w;  // two particles of the cell itself
-    bad = !(a.w <= 3.0e38f);
-    for (int g = 0; g <= r; g++) {
-      int cz = iz + g;
-      if (T.mode & M_PER_Z) cz = wrap_index(cz, T.nz);
-      else if (cz >= T.nz) break;
-      for (int l = g == 0 ? 0 : -r; l <= r; l++) {
-        int cy = iy + l;
-        if (T.mode & M_PER_Y) cy = wrap_index(cy, T.ny);
-        else if (cy < 0 || cy >= T.ny) continue;
-        for (int k = (g == 0 && l == 0) ? 1 : -r; k <= r; k++) {
-          const int cx = ix + k;
-          if (cx < 0 || cx >= T.nx) continue;
-          const float4 b = stat[kb + cx + cy * T.sy + cz * T.sz];
-          if (b.w < 0.0f) continue;
+    if (lane == 0) {
+      m = 2.0f * a.w;  // two particles of the cell itself
+      bad = !(a.w <= 3.0e38f);
+    }
+    // cube index idx = ((g + r) w + l + r) w + k + r; a lane starts at the
+    // centre + 1 + lane and steps by 32, its (g, l, k) advanced with carries
+    // (no division in the loop); |offsets| <= r < a periodic axis's cells, so
+    // one wrap brings a periodic index back
+    const int w = 2 * r + 1, n3 = w * w * w;
+    int idx = n3 / 2 + 1 + lane;
+    int k = idx % w - r, l = (idx / w) % w - r, g = idx / (w * w) - r;  // g >= 0 after the centre
+    const int sk = 32 % w, sl = (32 / w) % w, sg = 32 / (w * w);
+    for (; idx < n3; idx += 32) {
+      int cz = iz + g, cy = iy + l;
+      const int cx = ix + k;
+      if (T.mode & M_PER_Z) cz += cz < 0 ? T.nz : (cz >= T.nz ? -T.nz : 0);
+      if (T.mode & M_PER_Y) cy += cy < 0 ? T.ny : (cy >= T.ny ? -T.ny : 0);
+      if (cz < T.nz && cy >= 0 && cy < T.ny && cx >= 0 && cx < T.nx) {
+        const float4 b = stat[kb + cx + cy * T.sy + cz * T.sz];
+        if (b.w >= 0.0f) {
           const float ex = a.x - b.x, ey = a.y - b.y, ez = a.z - b.z;
           const float bound = a.w + b.w + sqrtf(ex * ex + ey * ey + ez * ez);
           bad |= !(bound <= 3.0e38f);
           m = fmaxf(m, bound);
         }
       }
+      k += sk;
+      l += sl;
+      g += sg;
+      if (k > r) { k -= w; ++l; }
+      if (l > r) { l -= w; ++g; }
     }
   }
-  warp_atomic_max(act ? &ts[t].disp_bits : nullptr, bad ? 0x7f800000u : __float_as_uint(m));
+  // m >= 0: its bits order as the floats do
+  const unsigned mb = __reduce_max_sync(FULL, __float_as_uint(m));
+  const unsigned v = __any_sync(FULL, bad) ? 0x7f800000u : mb;
+  if (act && lane == 0) {
+    if (t == s_tube) {
+      atomicMax(&s_acc, v);
+      s_any = 1;
+    } else {
+      atomicMax(&ts[t].disp_bits, v);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_any) atomicMax(&ts[s_tube].disp_bits, s_acc);
 }
 
 // per tube: re-sort and record this step, or keep the lists; *any: some tube
@@ -1170,8 +1209,8 @@ void ds_launch_list_test(const TubeDesc *tubes, TubeState *ts, int ntubes, const
     const int b = blocks_for(nkeys, 128);
     k_list_cellstat<<<b, 128, 0, s>>>(tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, cell_start, xl,
                                       disp, cellstat, force);
-    k_list_bound<<<b, 128, 0, s>>>(tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, krad, cellstat,
-                                   force);
+    k_list_bound<<<blocks_for(nkeys, DS_BOUND_WARPS), 32 * DS_BOUND_WARPS, 0, s>>>(
+        tubes, ts, nseg_key0, nseg_tube, nseg_species, nseg, nkeys, krad, cellstat, force);
   }
   k_list_decide<<<1, 256, 0, s>>>(tubes, ts, ntubes, force, any);
 }
