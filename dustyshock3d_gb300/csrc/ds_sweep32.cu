@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
 // screen of candidates.  Warps flagged as overflowed are left to the walk
 // (k_density32), tubes that re-sort to the recording walk.
 #ifndef DS_DPIECE
-#define DS_DPIECE 4  // list entries per pipeline stage of the density stream (measured: 4 beats 2 and 8)
+#define DS_DPIECE 4  // list entries per pipeline stage of the density stream (measured: 4 beats 2 and 8;
+                     // a piece-ahead prefetch as in the force list sweep measured 2 % slower here)
 #endif
 template <bool HPP>
 __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a) {
@@ -398,14 +399,14 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32(SweepArgs a) {
 
 // Force sweep over the recorded lists: no cell walk; entries in the walk's
 // order, each tested against its exact cut-off, so the sums equal the walk's.
-#ifndef DS_FPIECE
-#define DS_FPIECE 2  // list entries per pipeline stage (measured: 2 beats 4)
-#endif
-#ifndef DS_FLIST_MINB
-#define DS_FLIST_MINB 7  // blocks per SM the force list kernel is built for (measured: 7 beats 6 and 8)
-#endif
+// Measured on the 720k tube: the one-entry-deep prefetch took the force phase
+// from 0.548 to 0.478 ms per step with a 0.15 h skin (0.468 -> 0.421 ms
+// without), against the earlier two-entry pieces whose partner data loaded
+// only at the top of each piece; with it the kernel runs best unconstrained
+// (93 registers, 5 blocks per SM) -- built for 7 or 8 blocks per SM it spills
+// and measured 0.497 and 0.529 ms.
 template <bool HPP>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS, DS_FLIST_MINB) k_force32_list(SweepArgs a) {
+__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_force32_list(SweepArgs a) {
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
   __shared__ int claim;
@@ -424,38 +425,38 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, DS_FLIST_MINB) k_force32_lis
     const int cnt = act ? a.nbl_cnt[i] : 0;
     const int cnt_w = __reduce_max_sync(FULL, cnt);
     const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
-    // software pipeline: the next piece's entries load while this piece's
-    // neighbour data loads, before any of its pair work
-    uint32_t ent[DS_FPIECE];
-#pragma unroll
-    for (int t = 0; t < DS_FPIECE; t++) ent[t] = t < cnt ? __ldcs(nl + (size_t)t * DS_SWEEP_THREADS) : 0u;
-    for (int e = 0; e < cnt_w; e += DS_FPIECE) {
-      float4 pj[DS_FPIECE], vmj[DS_FPIECE], hyj[DS_FPIECE];
-#pragma unroll
-      for (int t = 0; t < DS_FPIECE; t++)
-        if (e + t < cnt) {
-          const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
-          pj[t] = a.pos32[j];
-          vmj[t] = a.vm32[j];
-          hyj[t] = a.hyd32[j];
-        }
-      uint32_t nxt[DS_FPIECE];
-#pragma unroll
-      for (int t = 0; t < DS_FPIECE; t++) {
-        const int q = e + DS_FPIECE + t;
-        nxt[t] = q < cnt ? __ldcs(nl + (size_t)q * DS_SWEEP_THREADS) : 0u;
+    // software pipeline, one entry deep: while entry e's pair work runs, the
+    // partner data of entry e + 1 and the index of entry e + 2 are in flight
+    // (pairs still summed in list order)
+    {
+      uint32_t e0 = 0u < (unsigned)cnt ? __ldcs(nl) : 0u;
+      uint32_t e1 = 1 < cnt ? __ldcs(nl + DS_SWEEP_THREADS) : 0u;
+      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), v0 = p0, y0 = p0;
+      if (0 < cnt) {
+        const int j = sb + (int)(e0 & DS_SLOT32_MASK);
+        p0 = a.pos32[j];
+        v0 = a.vm32[j];
+        y0 = a.hyd32[j];
       }
-#pragma unroll
-      for (int t = 0; t < DS_FPIECE; t++)
-        if (e + t < cnt) {
-          // the recorded cut-off may exceed this step's (list reuse: by the
-          // skin), and the particle itself is listed; the screen keeps
-          // exactly the pairs the walk's screen would
-          const float4 sh = shtab[ent[t] >> DS_OFS32_SHIFT];
-          if (F.screen(pj[t], sh.x - F.pi.x, sh.y - F.pi.y, sh.z - F.pi.z)) F.pair(sh, pj[t], vmj[t], hyj[t]);
+      for (int e = 0; e < cnt_w; e++) {
+        float4 p1 = p0, v1 = v0, y1 = y0;
+        if (e + 1 < cnt) {
+          const int j = sb + (int)(e1 & DS_SLOT32_MASK);
+          p1 = a.pos32[j];
+          v1 = a.vm32[j];
+          y1 = a.hyd32[j];
         }
-#pragma unroll
-      for (int t = 0; t < DS_FPIECE; t++) ent[t] = nxt[t];
+        const uint32_t e2 = e + 2 < cnt ? __ldcs(nl + (size_t)(e + 2) * DS_SWEEP_THREADS) : 0u;
+        if (e < cnt) {
+          const float4 sh = shtab[e0 >> DS_OFS32_SHIFT];
+          if (F.screen(p0, sh.x - F.pi.x, sh.y - F.pi.y, sh.z - F.pi.z)) F.pair(sh, p0, v0, y0);
+        }
+        e0 = e1;
+        e1 = e2;
+        p0 = p1;
+        v0 = v1;
+        y0 = y1;
+      }
     }
     if (act) F.store(a, i);
   }
