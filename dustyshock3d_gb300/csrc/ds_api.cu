@@ -582,7 +582,9 @@ __device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *
                           src.rho, src.p, src.e, src.m, src.h, src.ts};
   double *df[NF] = {dst.x, dst.y, dst.z, dst.vx, dst.vy, dst.vz, dst.ax, dst.ay, dst.az,
                     dst.rho, dst.p, dst.e, dst.m, dst.h, dst.ts};
-  if (!B.bound) {
+  // a segment without host arrays keeps its slot order, except with list reuse
+  // (EARLY), whose test and sort read every segment in caller order
+  if (!B.bound && !EARLY) {
 #pragma unroll
     for (int f = 0; f < NF; f++)
       if (bound_part<EARLY>(f) == PART) df[f][i] = sf[f][i];
@@ -593,6 +595,7 @@ __device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *
   const int p = i - tubes[ch.tube].seg_begin[ch.species];
   const int q = inv[i];  // the resident slot of particle p
   double v[NF];          // every load before any store: the link's latency is paid once
+  // (a segment without host arrays has no host fields: every one from q)
 #pragma unroll
   for (int f = 0; f < NF; f++)
     if (bound_part<EARLY>(f) == PART) v[f] = B.f[f] ? B.f[f][p] : sf[f][q];

@@ -218,3 +218,26 @@ def test_host_edit_of_h_or_ind_forces_a_rebuild(field):
         for f in ("x", "vx", "rho", "e"):
             a, b = bound[0][0][f], ref[0][f]
             assert np.abs(a - b).sum() <= 1e-5 * np.abs(b).sum() + 1e-30, f
+
+
+def test_partial_binding_with_list_reuse_equals_resident_steps():
+    """With list reuse and only the gas bound (the dust resident), bound steps
+    still equal resident steps bit for bit: the unbound dust is gathered in
+    caller order with the host's gas, so the test and the sort see every
+    species through the resident order."""
+    P, sp = _reuse_tube(0.15)
+    with Solver(P) as A, Solver(P) as B:
+        A.set_tube(0, sp)
+        B.set_tube(0, sp)
+        gas = _bind(B, _host_state(sp)[:1])
+        for step in range(8):
+            A.step(1)
+            B.step_host(1)
+            got = A.get_species(0, 0)
+            for f in GAS_OUT:
+                assert np.array_equal(gas[0][0][f], getattr(got, f)), f"step {step + 1} gas {f}"
+            for f in DUST_OUT:
+                assert np.array_equal(getattr(B.get_species(0, 1), f), getattr(A.get_species(0, 1), f)), \
+                    f"step {step + 1} dust {f}"
+        assert A.list_stats(0) == B.list_stats(0)
+        assert B.list_stats(0)[0] < 8
