@@ -98,6 +98,7 @@ struct ds_ctx {
   const uint32_t *skey = nullptr;  // sorted neighbour keys of the current order
   bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
+  float4 *pm32 = nullptr;  // with list reuse: coordinates and mass in one record (the density stream)
   double *cs64 = nullptr, *pt64 = nullptr, *dwn64 = nullptr, *edot = nullptr;
   uint32_t *nbl = nullptr;  // FP32 force neighbour lists, nbl_cap entries per gas slot of each chunk
   int *nbl_cnt = nullptr;
@@ -367,6 +368,7 @@ SweepArgs sweep_args(ds_ctx *c, const Chunk *chunks, int nchunks) {
   a.cell_start = c->cell_start;
   a.pos32 = c->pos32;
   a.vm32 = c->vm32;
+  a.pm32 = c->pm32;
   a.hyd32 = c->hyd32;
   a.cs64 = c->cs64;
   a.pt64 = c->pt64;
@@ -451,7 +453,7 @@ void enqueue_sort(ds_ctx *c, bool exact_order = false, cudaEvent_t before_reorde
   if (before_reorder) cudaStreamWaitEvent(s, before_reorder, 0);  // fields still arriving from the host
   ds_launch_reorder(c->d_tubes, c->d_ch_all, (int)c->ch_all.size(), sval, skey, src, dst, c->pos32, c->vm32,
                     c->idic_local, c->ikin, c->ivin, c->slot_of_pid, c->ind_of_pid, c->d_flags, fast, s, rts,
-                    (c->reuse && fast) ? c->pos_ref : nullptr, sp);
+                    (c->reuse && fast) ? c->pos_ref : nullptr, sp, fast ? c->pm32 : nullptr);
   ds_launch_cell_start(skey, c->N, c->nkeys << xl, c->cell_start, s, run_if);
   c->skey = skey;
   if (c->any_stencil2)
@@ -805,6 +807,7 @@ ds_status finalize(ds_ctx *c) {
     CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->e_wjoin, cudaEventDisableTiming));
     for (const auto &T : c->tdesc) c->reuse = c->reuse || T.skin > 0.0;
+    if (c->reuse) DA(c->pm32, N);  // the streamed density gathers one 16-byte record per partner
   }
   c->persistent = c->any_fp32 && c->params[0].persistent != 0;
   DA(c->d_work, DS_NSWEEP);

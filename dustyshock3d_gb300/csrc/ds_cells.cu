@@ -127,7 +127,7 @@ template <bool FAST>
 __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                           const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32,
                           int *idic_local, uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid,
-                          int *flags, const TubeState *ts, float4 *pos_ref, const int *slot_pid) {
+                          int *flags, const TubeState *ts, float4 *pos_ref, const int *slot_pid, float4 *pm32) {
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const Chunk ch = chunks[c];
     const int q = ch.begin + threadIdx.x;
@@ -197,6 +197,7 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     // FP32 copies converted on the integer pipe (ds_d2f: the IEEE conversion)
     p4.w = ds_d2f(h);
     pos32[q] = p4;
+    if (pm32) pm32[q] = make_float4(p4.x, p4.y, p4.z, ds_d2f(m));
     if (pos_ref && !keep) pos_ref[q] = p4;
     vm32[q] = make_float4(ds_d2f(vx), ds_d2f(vy), ds_d2f(vz), ds_d2f(m));
     const int ic = FAST ? fast_idic_cell(T, x, y, z) : ds_idic_cell(T, x, y, z);
@@ -1182,16 +1183,17 @@ void ds_launch_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, Dev
 void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const uint32_t *order,
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
-                       cudaStream_t s, const TubeState *reuse_ts, float4 *pos_ref, const int *slot_pid) {
+                       cudaStream_t s, const TubeState *reuse_ts, float4 *pos_ref, const int *slot_pid,
+                       float4 *pm32) {
   if (!nchunks) return;
   if (fast)
     k_reorder<true><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
                                                  idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, reuse_ts,
-                                                 pos_ref, slot_pid);
+                                                 pos_ref, slot_pid, pm32);
   else
     k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
                                                   idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, nullptr,
-                                                  nullptr, nullptr);
+                                                  nullptr, nullptr, nullptr);
 }
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if) {

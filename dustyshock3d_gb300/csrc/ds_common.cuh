@@ -599,6 +599,7 @@ struct SweepArgs {
   const int *cell_start;    // [nkeys + 1]
   const float4 *pos32;      // prefilter / FP32 coordinates + h
   const float4 *vm32;       // FP32 vx, vy, vz, m
+  const float4 *pm32;       // with list reuse: FP32 coordinates + m (the streamed density's partners), else nullptr
   float4 *hyd32;            // FP32 c, p/rho^2, rho, (unused) -- written by density
   double *cs64;             // sqrt(gam p / rho) per gas slot -- written by density
   double *pt64;             // p / (rho rho) per gas slot     -- written by density

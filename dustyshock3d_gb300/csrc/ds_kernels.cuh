@@ -35,7 +35,7 @@ void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
                        const uint32_t *skey, DevState src, DevState dst, float4 *pos32, float4 *vm32, int *idic_local,
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
                        cudaStream_t s, const TubeState *reuse_ts = nullptr, float4 *pos_ref = nullptr,
-                       const int *slot_pid = nullptr);
+                       const int *slot_pid = nullptr, float4 *pm32 = nullptr);
 // run_if: skipped when *run_if == 0 (no tube re-sorted this step)
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if = nullptr);

