@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(32 * DS_BOUND_WARPS)
   if (act && lane == 0) {
     if (t == s_tube) {
       atomicMax(&s_acc, v);
-      s_any = 1;
+      atomicOr(&s_any, 1);
     } else {
       atomicMax(&ts[t].disp_bits, v);
     }
