@@ -22,6 +22,8 @@ Reported (one JSON line from rank 0):
   reference_gpu the reference's own CUDA kernels (compiled unmodified into a
              cubin where the reference tree exists) under a restatement of its
              host loop, on its default run, beside the FP64 path on that run
+  serve      the served stream: 64 Poisson requests, continuous batching,
+             p50 / p99 time to solution (--workload serve adds comparators)
 
 --impl reference times the reference algorithm on the host cores (the oracle,
 a CPU restatement of the reference's step).
@@ -77,6 +79,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="default line: skip the 64-tube batch record")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="default line: skip the reference's own CUDA kernels on its default run")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="default line: skip the served stream (64 Poisson requests, no comparators)")
     ap.add_argument("--t-end", type=float, default=0.2, help="accuracy_720k: end time of every run")
     ap.add_argument("--list-skin", type=float, default=DEFAULT_SKIN,
                     help="FP32 legs of the default line: reuse the recorded neighbour lists across steps with this "
@@ -690,6 +694,9 @@ def run_ours(args):
     ref_gpu_rec = None
     if not args.no_ref_gpu and name == DEFAULT_WORKLOAD and rank == 0:
         ref_gpu_rec = reference_gpu_record()
+    serve_rec = None
+    if not args.no_serve and name == DEFAULT_WORKLOAD and ws == 1:
+        serve_rec = serve_record(args.seed, args.rate, args.requests)
     clk = clocks.stop()
 
     if rank != 0:
@@ -751,7 +758,7 @@ def run_ours(args):
             "phase_ms_per_step": {k: v / args.steps for k, v in zip(("sort", "density", "force", "idic_update"),
                                                                      phase)},
             "fp64": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "dusty_sod_5760k": c3, "batch64": batch, "reference_gpu": ref_gpu_rec,
+            "dusty_sod_5760k": c3, "batch64": batch, "reference_gpu": ref_gpu_rec, "serve": serve_rec,
             "gpu_launches": kps * args.steps, "clocks": clk}
     if args.list_skin > 0:
         line["list_reuse"] = {"skin_h": args.list_skin, "steps": list_steps, "steps_that_rebuilt": list_rebuilds,
@@ -789,6 +796,35 @@ def run_batch(args):
     return 0
 
 
+def serve_summary(res, wall, rebuilds=None, rebuild_s=None):
+    """Throughput and p50 / p99 time to solution of served (or one-at-a-time) results."""
+    import numpy as np
+    tts = np.array([r.time_to_solution for r in res])
+    ps = sum(r.particles * r.steps for r in res)
+    out = {"requests": len(res), "wall_s": wall, "particle_steps": ps, "value": ps / wall,
+           "p50_time_to_solution_s": float(np.percentile(tts, 50)),
+           "p99_time_to_solution_s": float(np.percentile(tts, 99))}
+    if rebuilds is not None:
+        out.update(rebuilds=rebuilds, rebuild_s=rebuild_s, rebuild_ms_each=1e3 * rebuild_s / max(rebuilds, 1))
+    return out
+
+
+def serve_record(seed, rate=4.0, requests=64):
+    """The served stream of the serve workload without its comparators: 64
+    Poisson requests of uneven tubes generated on the device at admission,
+    continuous batching under 150 GB, epochs of 10 steps."""
+    from dustyshock3d_gb300.serve import Server, device_uneven_tube, poisson_requests
+    reqs = poisson_requests(rate, requests, seed, device_uneven_tube)
+    server = Server(budget_bytes=150e9, epoch_steps=10, precision="fp32")
+    t0 = time.perf_counter()
+    res = server.run(reqs)
+    rec = serve_summary(res, time.perf_counter() - t0, server.rebuilds, server.rebuild_s)
+    rec.update(workload="serve", rate_per_s=rate, seed=seed, budget_bytes=150e9, epoch_steps=10,
+               note="python bench.py --workload serve adds the comparators (the first 16 requests served alone "
+                    "and solved one at a time on FP32 and FP64)")
+    return rec
+
+
 def run_serve(args):
     """Poisson stream of uneven tubes, continuous batching under 150 GB.
 
@@ -796,8 +832,6 @@ def run_serve(args):
     arrival times) served on their own, then solved one at a time in arrival
     order on the FP32 path and on the plain FP64 path (ds_step of one tube per
     context, a request waiting while the previous one runs)."""
-    import numpy as np
-
     from dustyshock3d_gb300 import ic
     from dustyshock3d_gb300.serve import Server, device_uneven_tube, one_at_a_time, poisson_requests
     if args.host_ic:  # initial particles made on the host and uploaded at admission
@@ -806,15 +840,7 @@ def run_serve(args):
         make = device_uneven_tube
     reqs = poisson_requests(args.rate, args.requests, args.seed, make)
 
-    def summary(res, wall, rebuilds=None, rebuild_s=None):
-        tts = np.array([r.time_to_solution for r in res])
-        ps = sum(r.particles * r.steps for r in res)
-        out = {"requests": len(res), "wall_s": wall, "particle_steps": ps, "value": ps / wall,
-               "p50_time_to_solution_s": float(np.percentile(tts, 50)),
-               "p99_time_to_solution_s": float(np.percentile(tts, 99))}
-        if rebuilds is not None:
-            out.update(rebuilds=rebuilds, rebuild_s=rebuild_s, rebuild_ms_each=1e3 * rebuild_s / max(rebuilds, 1))
-        return out
+    summary = serve_summary
 
     clocks = ClockSampler(0)
     clocks.start()
