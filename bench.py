@@ -918,6 +918,8 @@ def run_accuracy(args):
     def run(P, sp, prec):
         Q = P.copy()
         Q.precision = prec
+        if prec == "fp32":
+            Q.list_skin = args.list_skin  # the default line's FP32 configuration
         with Solver(Q) as S:
             S.set_tube(0, sp)
             ms_tot, groups = 0.0, 0
@@ -968,6 +970,7 @@ def run_accuracy(args):
     keys = ("l1_rho_gas", "l1_v_gas", "l1_v_dust", "l1_profile_rho_gas", "l1_profile_v_gas", "l1_profile_v_dust")
     ratios = [v for r in rows if "exact" in r for v in r["exact"]["fp32_over_fp64"].values()]
     line = {"metric": "l1 error, fp32 path vs fp64 path", "workload": "accuracy_720k", "t_end": args.t_end,
+            "fp32_list_skin_h": args.list_skin,
             "particles": n, "rows": rows, "max": {k: max(r[k] for r in rows) for k in keys},
             "exact_fp32_over_fp64": {"min": min(ratios), "max": max(ratios)} if ratios else None,
             "fp64_floor": floor,
