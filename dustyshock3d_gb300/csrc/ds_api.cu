@@ -99,6 +99,8 @@ struct ds_ctx {
   bool any_stencil2 = false;
   float4 *pos32 = nullptr, *vm32 = nullptr, *hyd32 = nullptr;
   float4 *pm32 = nullptr;  // with list reuse: coordinates and mass in one record (the density stream)
+  float2 *dsum = nullptr;  // with list reuse: a bound step's early density sums (Kahan pairs)
+  bool dens_split = false;  // set while a bound step with list reuse is enqueued
   double *cs64 = nullptr, *pt64 = nullptr, *dwn64 = nullptr, *edot = nullptr;
   uint32_t *nbl = nullptr;  // FP32 force neighbour lists, nbl_cap entries per gas slot of each chunk
   int *nbl_cnt = nullptr;
@@ -478,7 +480,10 @@ void enqueue_density(ds_ctx *c, cudaEvent_t *ev) {
   const int depth = c->params[0].list_depth;
   if (fp32) ds_launch_density32(ag, c->any_hpp, 0, depth, s);
   else ds_launch_density64(ag, c->any_hpp, c->any_proper, 0, s);
-  if (fp32 && c->reuse) ds_launch_density32_lst(ag, c->any_hpp, s);  // tubes keeping their lists
+  if (fp32 && c->reuse) {  // tubes keeping their lists
+    if (c->dens_split) ds_launch_density32_lst_finish(ag, c->any_hpp, c->dsum, s);  // sums taken before the reorder
+    else ds_launch_density32_lst(ag, c->any_hpp, s);
+  }
   if (c->any_dust_rho) {
     if (fp32) ds_launch_density32(ad, c->any_hpp, 1, depth, s);
     else ds_launch_density64(ad, c->any_hpp, c->any_proper, 1, s);
@@ -567,11 +572,12 @@ __global__ void k_inverse(const Chunk *chunks, const TubeDesc *tubes, const int 
 // Into the other buffer set in caller order (slot seg_begin + p = particle p):
 // bound fields from the host, unbound ones gathered from the resident state;
 // segments without host arrays carried over slot for slot.  PART 0: x, y, z
-// and pid (what the cell keys read), and with EARLY also h and Ind (what the
-// list-reuse test reads); PART 1: the other fields.
+// and pid (what the cell keys read), and with EARLY also h, the mass and Ind
+// (what the list-reuse test and the early density sums read); PART 1: the
+// other fields.
 template <bool EARLY>
 __host__ __device__ constexpr int bound_part(int f) {
-  return (f == FX || f == FY || f == FZ || (EARLY && f == FH)) ? 0 : 1;
+  return (f == FX || f == FY || f == FZ || (EARLY && (f == FH || f == FM))) ? 0 : 1;
 }
 template <int PART, bool EARLY>
 __device__ __forceinline__ void bound_in_chunk(const Chunk &ch, const TubeDesc *tubes, const BoundSeg *bs,
@@ -685,12 +691,20 @@ void enqueue_bound_step(ds_ctx *c) {
     ds_launch_list_test(c->d_tubes, c->d_tstate, c->ntubes, c->d_ch_gas, (int)c->ch_gas.size(), neu, fast_skey(c),
                         c->pos_ref, c->disp, c->d_nseg_key0, c->d_nseg_tube, c->d_nseg_species, c->nnseg, c->nkeys,
                         c->cell_start, c->xl, c->krad, c->cellstat, c->d_force, c->d_any, s, old.pid, old);
+    // the tubes that keep their lists take their density sums now, from the
+    // positions, h and masses already here, while the second stream still
+    // brings the other fields; the rest of the sweep follows the reorder
+    ds_launch_early_fp32(c->d_tubes, c->d_ch_gas, (int)c->ch_gas.size(), c->d_tstate, fast_skey(c), neu, old.pid,
+                         c->pos32, c->pm32, s);
+    ds_launch_density32_lst_sums(gas_sweep_args(c), c->any_hpp, neu, old.pid, c->dsum, s);
+    c->dens_split = true;
     enqueue_sort(c, false, c->e_up, true, old.pid);
   } else {
     enqueue_sort(c, false, c->e_up);  // the host's arrays: every tube re-sorts
   }
   k_inverse<<<nch, DS_CHUNK, 0, s>>>(c->d_ch_all, c->d_tubes, c->buf[c->parity].pid, c->inv);
   enqueue_physics(c, nullptr, c->e_dens, c->e_force);
+  c->dens_split = false;
   DevState st = c->buf[c->parity].view();
   cudaStreamWaitEvent(s2, c->e_dens, 0);
   k_bound_out<0><<<nside, DS_CHUNK, 0, s2>>>(c->d_ch_all, nch, c->d_tubes, c->d_bound, c->inv, st);
@@ -807,7 +821,10 @@ ds_status finalize(ds_ctx *c) {
     CK(cudaEventCreateWithFlags(&c->e_wfork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->e_wjoin, cudaEventDisableTiming));
     for (const auto &T : c->tdesc) c->reuse = c->reuse || T.skin > 0.0;
-    if (c->reuse) DA(c->pm32, N);  // the streamed density gathers one 16-byte record per partner
+    if (c->reuse) {
+      DA(c->pm32, N);  // the streamed density gathers one 16-byte record per partner
+      DA(c->dsum, N);
+    }
   }
   c->persistent = c->any_fp32 && c->params[0].persistent != 0;
   DA(c->d_work, DS_NSWEEP);

@@ -113,6 +113,74 @@ __global__ void k_keys(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
   }
 }
 
+// FP32 coordinates of a slot's particle: offsets from the own (listed) cell's
+// origin (proper grid), or from the tube's reference point (reference grid).
+// FP32 path: x relative to the x-block origin (row walks), y, z to the cell's;
+// the origins of grid cells from the tube's table (the same FP64 values,
+// without the FP64 multiply-adds); a particle of a tube that kept its lists
+// may have wrapped through a periodic face since its cell was set.  Shared by
+// the reorder and the early FP32 copies of a bound step, so both give the
+// same bits.
+template <bool FAST>
+__device__ __forceinline__ float4 slot_offsets(const TubeDesc &T, int species, uint32_t key, double x, double y,
+                                               double z, bool keep) {
+  float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (T.cellrel) {
+    const int local = (int)(key >> (FAST ? T.xl : 0)) - T.key_base[species];
+    int ix, iy, iz;
+    if (local < T.ncells) {
+      ix = local % T.nx;
+      iy = (local / T.nx) % T.ny;
+      iz = local / (T.nx * T.ny);
+    } else if (FAST) {
+      ds_fast_proper_cell(T, x, y, z, ix, iy, iz);
+    } else {
+      ds_proper_cell(T, x, y, z, ix, iy, iz);
+    }
+    const int bx = FAST ? ((ix >> DS_XB_LOG) << DS_XB_LOG) : ix;
+    if (FAST && local < T.ncells) {
+      p4.x = ds_d2f(x - T.orig[ix >> DS_XB_LOG]);
+      double dy = y - T.orig[T.nbx + iy], dz = z - T.orig[T.nbx + T.ny + iz];
+      if (keep) {
+        if (T.mode & M_PER_Y) dy += dy > 0.5 * T.Ly ? -T.Ly : (dy < -0.5 * T.Ly ? T.Ly : 0.0);
+        if (T.mode & M_PER_Z) dz += dz > 0.5 * T.Lz ? -T.Lz : (dz < -0.5 * T.Lz ? T.Lz : 0.0);
+      }
+      p4.y = ds_d2f(dy);
+      p4.z = ds_d2f(dz);
+    } else {
+      p4.x = ds_d2f(x - (T.ox + bx * T.wx));
+      p4.y = ds_d2f(y - (T.oy + iy * T.wy));
+      p4.z = ds_d2f(z - (T.oz + iz * T.wz));
+    }
+  } else {
+    p4.x = ds_d2f(x - T.fx);
+    p4.y = ds_d2f(y - T.fy);
+    p4.z = ds_d2f(z - T.fz);
+  }
+  return p4;
+}
+
+// A bound step with list reuse (early, before the host's other fields have
+// arrived): the FP32 copies the streamed density reads -- pos32 (offsets and
+// h) and pm32 (offsets and mass) -- for the gas of the tubes that keep their
+// lists, from the host's positions, h and mass in caller order (slot q holds
+// particle slot_pid[q]).  The reorder later writes the same values.
+__global__ void k_early_fp32(const TubeDesc *tubes, const Chunk *chunks, int nchunks, const TubeState *ts,
+                             const uint32_t *skey, DevState cs, const int *slot_pid, float4 *pos32, float4 *pm32) {
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int q = ch.begin + threadIdx.x;
+    if (q >= ch.end || ts[ch.tube].rebuild) continue;
+    const TubeDesc &T = tubes[ch.tube];
+    const int j = T.seg_begin[ch.species] + slot_pid[q];
+    float4 p4 = slot_offsets<true>(T, ch.species, skey[q], cs.x[j], cs.y[j], cs.z[j], true);
+    const float mf = ds_d2f(cs.m[j]);
+    p4.w = ds_d2f(cs.h[j]);
+    pos32[q] = p4;
+    pm32[q] = make_float4(p4.x, p4.y, p4.z, mf);
+  }
+}
+
 // Gather every persistent field from the previous order (src) into the new
 // sorted order (dst); build the FP32 copies and the IDIC keys (reference
 // order: at the caller index, so the IDIC sums run in ascending index as the
@@ -156,45 +224,8 @@ __global__ void k_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunk
     const int gp = T.seg_begin[ch.species] + pid;
     if (!(T.mode & M_TSTOP_CONST)) slot_of_pid[gp] = q;  // index-coupled stopping time (IDIC.h:86)
     if (T.mode & M_REF_COUPLING) ind_of_pid[gp] = ind;    // index-coupled dust rho zeroing (IDIC.h:8)
-    // FP32 coordinates: offsets from the own (listed) cell's origin (proper
-    // grid), or from the tube's reference point (reference grid)
-    float4 p4;
-    if (T.cellrel) {
-      const int local = (int)(skey[q] >> (FAST ? T.xl : 0)) - T.key_base[ch.species];
-      int ix, iy, iz;
-      if (local < T.ncells) {
-        ix = local % T.nx;
-        iy = (local / T.nx) % T.ny;
-        iz = local / (T.nx * T.ny);
-      } else if (FAST) {
-        ds_fast_proper_cell(T, x, y, z, ix, iy, iz);
-      } else {
-        ds_proper_cell(T, x, y, z, ix, iy, iz);
-      }
-      // FP32 path: x relative to the x-block origin (row walks), y, z to the
-      // cell's; the origins of grid cells from the tube's table (the same FP64
-      // values, without the FP64 multiply-adds)
-      const int bx = FAST ? ((ix >> DS_XB_LOG) << DS_XB_LOG) : ix;
-      if (FAST && local < T.ncells) {
-        p4.x = ds_d2f(x - T.orig[ix >> DS_XB_LOG]);
-        double dy = y - T.orig[T.nbx + iy], dz = z - T.orig[T.nbx + T.ny + iz];
-        if (keep) {  // a kept particle may have wrapped through a periodic face since its cell was set
-          if (T.mode & M_PER_Y) dy += dy > 0.5 * T.Ly ? -T.Ly : (dy < -0.5 * T.Ly ? T.Ly : 0.0);
-          if (T.mode & M_PER_Z) dz += dz > 0.5 * T.Lz ? -T.Lz : (dz < -0.5 * T.Lz ? T.Lz : 0.0);
-        }
-        p4.y = ds_d2f(dy);
-        p4.z = ds_d2f(dz);
-      } else {
-        p4.x = ds_d2f(x - (T.ox + bx * T.wx));
-        p4.y = ds_d2f(y - (T.oy + iy * T.wy));
-        p4.z = ds_d2f(z - (T.oz + iz * T.wz));
-      }
-    } else {
-      p4.x = ds_d2f(x - T.fx);
-      p4.y = ds_d2f(y - T.fy);
-      p4.z = ds_d2f(z - T.fz);
-    }
     // FP32 copies converted on the integer pipe (ds_d2f: the IEEE conversion)
+    float4 p4 = slot_offsets<FAST>(T, ch.species, skey[q], x, y, z, keep);
     p4.w = ds_d2f(h);
     pos32[q] = p4;
     if (pm32) pm32[q] = make_float4(p4.x, p4.y, p4.z, ds_d2f(m));
@@ -1194,6 +1225,12 @@ void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
     k_reorder<false><<<nchunks, DS_CHUNK, 0, s>>>(tubes, chunks, nchunks, order, skey, src, dst, pos32, vm32,
                                                   idic_local, ikin, ivin, slot_of_pid, ind_of_pid, flags, nullptr,
                                                   nullptr, nullptr, nullptr);
+}
+void ds_launch_early_fp32(const TubeDesc *tubes, const Chunk *gas_chunks, int ngas_chunks, const TubeState *ts,
+                          const uint32_t *skey, DevState cs, const int *slot_pid, float4 *pos32, float4 *pm32,
+                          cudaStream_t s) {
+  if (ngas_chunks)
+    k_early_fp32<<<ngas_chunks, DS_CHUNK, 0, s>>>(tubes, gas_chunks, ngas_chunks, ts, skey, cs, slot_pid, pos32, pm32);
 }
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if) {

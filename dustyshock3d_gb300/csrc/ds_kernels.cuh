@@ -36,6 +36,12 @@ void ds_launch_reorder(const TubeDesc *tubes, const Chunk *chunks, int nchunks, 
                        uint32_t *ikin, uint32_t *ivin, int *slot_of_pid, int *ind_of_pid, int *flags, bool fast,
                        cudaStream_t s, const TubeState *reuse_ts = nullptr, float4 *pos_ref = nullptr,
                        const int *slot_pid = nullptr, float4 *pm32 = nullptr);
+// A bound step with list reuse: pos32 and pm32 of the gas of the tubes that
+// keep their lists, from the host's state in caller order (slot q holds
+// particle slot_pid[q]), before the reorder.
+void ds_launch_early_fp32(const TubeDesc *tubes, const Chunk *gas_chunks, int ngas_chunks, const TubeState *ts,
+                          const uint32_t *skey, DevState cs, const int *slot_pid, float4 *pos32, float4 *pm32,
+                          cudaStream_t s);
 // run_if: skipped when *run_if == 0 (no tube re-sorted this step)
 void ds_launch_cell_start(const uint32_t *skey, int n, int nkeys, int *cell_start, cudaStream_t s,
                           const int *run_if = nullptr);
@@ -94,5 +100,11 @@ void ds_launch_force32_walk(const SweepArgs &a, bool hpp, int depth, cudaStream_
 void ds_sweep32_blocks_per_sm(bool hpp, int depth, bool list, int *bps);
 // list reuse: the density of tubes keeping their lists, streamed from them
 void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s);
+// The density stream split for a step on bound host arrays: the sums before
+// the reorder (cs: the host's state in caller order, slot i holding particle
+// slot_pid[i]; Kahan pairs into dsum), the density and the rest after it.
+void ds_launch_density32_lst_sums(const SweepArgs &a, bool hpp, DevState cs, const int *slot_pid, float2 *dsum,
+                                  cudaStream_t s);
+void ds_launch_density32_lst_finish(const SweepArgs &a, bool hpp, float2 *dsum, cudaStream_t s);
 // parity hook: one tube's recorded force lists by caller index (a: gas chunks)
 void ds_launch_debug_force_lists(const SweepArgs &a, int tube, int cap, int *count, int *nbr, cudaStream_t s);

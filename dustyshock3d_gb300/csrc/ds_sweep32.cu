@@ -229,8 +229,17 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS, LIST ? DS_DENS_LIST_MINB : (
 #define DS_DPIECE 4  // list entries per pipeline stage of the density stream (measured: 4 beats 2 and 8;
                      // a piece-ahead prefetch as in the force list sweep measured 2 % slower here)
 #endif
-template <bool HPP>
-__global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a) {
+//
+// MODE 0: the whole sweep (sums, then density, EOS, force inputs, CFL bound).
+// MODE 1 and 2 split it for a step on bound host arrays, so that the sums run
+// while the host's other fields are still on their way: MODE 1 (before the
+// reorder) reads a slot's own Ind and h from the host's state in caller order
+// (cs; slot i holds particle slot_pid[i]) and the FP32 copies of the early
+// pass, and stores each slot's Kahan pair in dsum; MODE 2 (after the reorder)
+// finishes from dsum exactly as MODE 0 does after its loop.
+template <bool HPP, int MODE>
+__global__ void __launch_bounds__(DS_SWEEP_THREADS)
+    k_density32_lst(SweepArgs a, DevState cs, const int *slot_pid, float2 *dsum) {
   const unsigned FULL = 0xffffffffu;
   __shared__ float4 shtab[DS_NOFS32];
   __shared__ int claim;
@@ -242,55 +251,71 @@ __global__ void __launch_bounds__(DS_SWEEP_THREADS) k_density32_lst(SweepArgs a)
     __syncthreads();
     ds_fill_shift_table32(T, shtab);
     __syncthreads();
+    const int sb = T.seg_begin[ch.species];
     const bool listed = !a.nbl_walk[c * (DS_SWEEP_THREADS / 32) + (threadIdx.x >> 5)];
     const bool valid = listed && i < ch.end && (a.all_tubes || a.tstate[ch.tube].active);
-    const bool upd = valid && a.st.ind[i] == 0;
-    double rho = valid ? a.st.rho[i] : 0.0;
-    if (upd) rho = 0.0;
-    const double hd = upd ? (HPP ? a.st.h[i] : T.h) : T.h;
+    const int jo = (MODE == 1 && valid) ? sb + slot_pid[i] : i;  // the slot's own particle in cs
+    const bool upd = valid && (MODE == 1 ? cs.ind[jo] : a.st.ind[i]) == 0;
+    double rho = 0.0;
+    if (MODE != 1) {
+      rho = valid ? a.st.rho[i] : 0.0;
+      if (upd) rho = 0.0;
+    }
+    const double hd = upd ? (HPP ? (MODE == 1 ? cs.h[jo] : a.st.h[i]) : T.h) : T.h;
     const float4 pi = upd ? a.pos32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float hf = (float)hd, inv_h = 1.0f / hf, cut2 = 4.0f * hf * hf;
-    const int sb = T.seg_begin[ch.species];
     Kahan sum;
-    const int cnt = upd ? a.nbl_cnt[i] : 0;
-    const int cnt_w = __reduce_max_sync(FULL, cnt);
-    const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
-    uint32_t ent[DS_DPIECE];
-#pragma unroll
-    for (int t = 0; t < DS_DPIECE; t++) ent[t] = t < cnt ? __ldcs(nl + (size_t)t * DS_SWEEP_THREADS) : 0u;
-    for (int e = 0; e < cnt_w; e += DS_DPIECE) {
-      float4 pj[DS_DPIECE];
-      float mj[DS_DPIECE];
-#pragma unroll
-      for (int t = 0; t < DS_DPIECE; t++)
-        if (e + t < cnt) {
-          const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
-          if (a.pm32) {  // coordinates and mass in one 16-byte record (measured: 0.496 -> 0.482 ms per step)
-            pj[t] = a.pm32[j];
-            mj[t] = pj[t].w;
-          } else {
-            pj[t] = a.pos32[j];
-            mj[t] = a.vm32[j].w;
-          }
-        }
-      uint32_t nxt[DS_DPIECE];
-#pragma unroll
-      for (int t = 0; t < DS_DPIECE; t++) {
-        const int q = e + DS_DPIECE + t;
-        nxt[t] = q < cnt ? __ldcs(nl + (size_t)q * DS_SWEEP_THREADS) : 0u;
+    if (MODE == 2) {
+      if (upd) {
+        const float2 k = dsum[i];
+        sum.s = k.x;
+        sum.c = k.y;
       }
+    } else {
+      const int cnt = upd ? a.nbl_cnt[i] : 0;
+      const int cnt_w = __reduce_max_sync(FULL, cnt);
+      const uint32_t *nl = a.nbl + (size_t)c * a.nbl_cap * DS_SWEEP_THREADS + threadIdx.x;
+      uint32_t ent[DS_DPIECE];
 #pragma unroll
-      for (int t = 0; t < DS_DPIECE; t++)
-        if (e + t < cnt) {
-          const float4 sh = shtab[ent[t] >> DS_OFS32_SHIFT];
-          const float r2 = r2_of(pj[t].x + (sh.x - pi.x), pj[t].y + (sh.y - pi.y), pj[t].z + (sh.z - pi.z));
-          if (r2 < cut2) {
-            const float q = r2 > 0.0f ? r2 * rsqrtf(r2) * inv_h : 0.0f;
-            sum.add(mj[t] * w_shape(q));
+      for (int t = 0; t < DS_DPIECE; t++) ent[t] = t < cnt ? __ldcs(nl + (size_t)t * DS_SWEEP_THREADS) : 0u;
+      for (int e = 0; e < cnt_w; e += DS_DPIECE) {
+        float4 pj[DS_DPIECE];
+        float mj[DS_DPIECE];
+#pragma unroll
+        for (int t = 0; t < DS_DPIECE; t++)
+          if (e + t < cnt) {
+            const int j = sb + (int)(ent[t] & DS_SLOT32_MASK);
+            if (a.pm32) {  // coordinates and mass in one 16-byte record (measured: 0.496 -> 0.482 ms per step)
+              pj[t] = a.pm32[j];
+              mj[t] = pj[t].w;
+            } else {
+              pj[t] = a.pos32[j];
+              mj[t] = a.vm32[j].w;
+            }
           }
+        uint32_t nxt[DS_DPIECE];
+#pragma unroll
+        for (int t = 0; t < DS_DPIECE; t++) {
+          const int q = e + DS_DPIECE + t;
+          nxt[t] = q < cnt ? __ldcs(nl + (size_t)q * DS_SWEEP_THREADS) : 0u;
         }
 #pragma unroll
-      for (int t = 0; t < DS_DPIECE; t++) ent[t] = nxt[t];
+        for (int t = 0; t < DS_DPIECE; t++)
+          if (e + t < cnt) {
+            const float4 sh = shtab[ent[t] >> DS_OFS32_SHIFT];
+            const float r2 = r2_of(pj[t].x + (sh.x - pi.x), pj[t].y + (sh.y - pi.y), pj[t].z + (sh.z - pi.z));
+            if (r2 < cut2) {
+              const float q = r2 > 0.0f ? r2 * rsqrtf(r2) * inv_h : 0.0f;
+              sum.add(mj[t] * w_shape(q));
+            }
+          }
+#pragma unroll
+        for (int t = 0; t < DS_DPIECE; t++) ent[t] = nxt[t];
+      }
+    }
+    if (MODE == 1) {
+      if (valid) dsum[i] = make_float2(sum.s, sum.c);
+      continue;
     }
     const unsigned dtb = valid ? density_epilogue<HPP, 0>(a, T, ch, i, upd, upd, rho, hd, hf, sum) : ~0u;
     cfl_min_warp(a, ch.tube, dtb);
@@ -495,8 +520,8 @@ __global__ void k_debug_force_lists(SweepArgs a, int tube, int cap, int *count, 
 
 // One sweep launch: one block per chunk, or (with work counters) a
 // persistent grid of nsm x bps[k] blocks claiming chunks from counter k.
-template <class Kernel>
-static void launch_sweep(Kernel kern, const SweepArgs &a, int k, cudaStream_t s) {
+template <class Kernel, class... Extra>
+static void launch_sweep(Kernel kern, const SweepArgs &a, int k, cudaStream_t s, Extra... extra) {
   SweepArgs b = a;
   int n = a.nchunks;
   if (b.work) {
@@ -504,7 +529,7 @@ static void launch_sweep(Kernel kern, const SweepArgs &a, int k, cudaStream_t s)
     const long long g = (long long)(a.bps[k] > 0 ? a.bps[k] : 1) * (a.nsm > 0 ? a.nsm : 1);
     n = (int)(g < n ? g : n);
   }
-  kern<<<n, DS_SWEEP_THREADS, 0, s>>>(b);
+  kern<<<n, DS_SWEEP_THREADS, 0, s>>>(b, extra...);
 }
 
 template <int CAP>
@@ -532,13 +557,13 @@ template <int CAP>
 static void fit_all(bool hpp, bool list, int *bps) {
   if (hpp) {
     bps[DS_SW_DENSITY] = list ? fit(k_density32<true, 0, CAP, true>) : fit(k_density32<true, 0, CAP, false>);
-    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<true>);
+    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<true, 0>);
     bps[DS_SW_DUST_DENSITY] = fit(k_density32<true, 1, CAP, false>);
     bps[DS_SW_FORCE_LIST] = fit(k_force32_list<true>);
     bps[DS_SW_FORCE_WALK] = fit(k_force32<true, CAP>);
   } else {
     bps[DS_SW_DENSITY] = list ? fit(k_density32<false, 0, CAP, true>) : fit(k_density32<false, 0, CAP, false>);
-    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<false>);
+    bps[DS_SW_DENSITY_LST] = fit(k_density32_lst<false, 0>);
     bps[DS_SW_DUST_DENSITY] = fit(k_density32<false, 1, CAP, false>);
     bps[DS_SW_FORCE_LIST] = fit(k_force32_list<false>);
     bps[DS_SW_FORCE_WALK] = fit(k_force32<false, CAP>);
@@ -558,8 +583,29 @@ void ds_launch_density32(const SweepArgs &a, bool hpp, int what, int depth, cuda
 
 void ds_launch_density32_lst(const SweepArgs &a, bool hpp, cudaStream_t s) {
   if (!a.nchunks || !a.nbl || !a.reuse) return;
-  if (hpp) launch_sweep(k_density32_lst<true>, a, DS_SW_DENSITY_LST, s);
-  else launch_sweep(k_density32_lst<false>, a, DS_SW_DENSITY_LST, s);
+  const DevState none{};
+  if (hpp) launch_sweep(k_density32_lst<true, 0>, a, DS_SW_DENSITY_LST, s, none, nullptr, nullptr);
+  else launch_sweep(k_density32_lst<false, 0>, a, DS_SW_DENSITY_LST, s, none, nullptr, nullptr);
+}
+
+// The same split for a step on bound host arrays: the sums before the
+// reorder (cs: the host's state in caller order, slot i holding particle
+// slot_pid[i]), the rest after it.  One block per chunk.
+void ds_launch_density32_lst_sums(const SweepArgs &a, bool hpp, DevState cs, const int *slot_pid, float2 *dsum,
+                                  cudaStream_t s) {
+  if (!a.nchunks || !a.nbl || !a.reuse) return;
+  SweepArgs b = a;
+  b.work = nullptr;
+  if (hpp) k_density32_lst<true, 1><<<b.nchunks, DS_SWEEP_THREADS, 0, s>>>(b, cs, slot_pid, dsum);
+  else k_density32_lst<false, 1><<<b.nchunks, DS_SWEEP_THREADS, 0, s>>>(b, cs, slot_pid, dsum);
+}
+void ds_launch_density32_lst_finish(const SweepArgs &a, bool hpp, float2 *dsum, cudaStream_t s) {
+  if (!a.nchunks || !a.nbl || !a.reuse) return;
+  SweepArgs b = a;
+  b.work = nullptr;
+  const DevState none{};
+  if (hpp) k_density32_lst<true, 2><<<b.nchunks, DS_SWEEP_THREADS, 0, s>>>(b, none, nullptr, dsum);
+  else k_density32_lst<false, 2><<<b.nchunks, DS_SWEEP_THREADS, 0, s>>>(b, none, nullptr, dsum);
 }
 
 void ds_launch_debug_force_lists(const SweepArgs &a, int tube, int cap, int *count, int *nbr, cudaStream_t s) {
