@@ -319,12 +319,14 @@ ds_status ds_synchronize(ds_ctx *c);
  * IDIC phase (kernels over NVLink-C2C on a second stream, all in one CUDA
  * graph).  Returns when the last step's results are in host memory.  Without
  * list reuse, results equal ds_upload_* + ds_step(1) + ds_download_* per
- * step, bit for bit (an upload re-sorts every tube).  With list reuse (list_skin > 0, FP32 path) a step reads h and Ind with the
+ * step, bit for bit (an upload re-sorts every tube).  With list reuse
+ * (list_skin > 0, FP32 path) a step reads h, the masses and Ind with the
  * positions, and the start-of-step test measures the host's positions against
  * the recorded ones: a tube keeps its lists and slot order as a step on the
- * resident state would, so steps on unchanged host arrays equal ds_step(1) per
- * step bit for bit; a host edit of any particle's h or Ind makes its tube
- * re-sort and record.
+ * resident state would (its density sums start before the other fields have
+ * arrived), so steps on unchanged host arrays equal ds_step(1) per step bit
+ * for bit; a host edit of any particle's h or Ind makes its tube re-sort and
+ * record.
  * fields == NULL unbinds the species.  ds_step / ds_get_* keep working on the
  * resident state in between. */
 ds_status ds_bind_host(ds_ctx *c, int tube, int species, int n, double *const *fields, int *ind);
